@@ -1,0 +1,312 @@
+"""Benchmark of the Nekbone CG hot path on one GB300.
+
+Workload (the headline metric's configuration): a 32x32x32 box of undeformed
+hexahedral elements, lx1=12 GLL points per direction (n = 56,623,104 local
+points), full Dirichlet mask, seeded uniform RHS; one step = one call of the
+reference's cg (cg.f:2-84): 100 plain FP64 CG iterations with the identity
+preconditioner.  Metric: GDOF*iter/s = n * 100 / seconds / 1e9 (the
+reference's DOF convention, n = nelt*lx1^3).
+
+  value  -- device-resident solve (inputs already in HBM), CUDA events on
+            the library's stream, K steps after W warm-up steps.  Every
+            vector (453 MB) is larger than L2 (129 MB).
+  e2e    -- the same solve through the drop-in C ABI call cg_ with pinned
+            HOST buffers: f, g, c copied in and x, r, w, p, z copied out inside
+            the timed region, every step.
+  roofline -- the dominant kernel (the fused element operator k_ax), from its
+            own CUDA-event time over a timed CG iteration loop.
+  mixed  -- time to relative residual 1e-10 of plain FP64 CG and of the
+            mixed-precision solver (FP32 inner CG in FP64 defect correction).
+  cpu_baseline -- the oracle (CPU restatement, OpenMP over elements) on the
+            host cores, on a bounded sample of the same workload.
+
+--impl reference runs the reference's CPU algorithm (the oracle port; the
+Fortran reference has no compiler in this image) on the same configuration.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GDOF·iter/s (lx1=12, 32^3 elems); mixed vs FP64 GPU time to rel. resid 1e-10"
+UNIT = "GDOF*iter/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nel", type=int, default=32, help="elements per direction")
+    ap.add_argument("--lx", type=int, default=12)
+    ap.add_argument("--niter", type=int, default=100)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--cpu-sample-nel", type=int, default=16)
+    ap.add_argument("--cpu-sample-iters", type=int, default=10)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), parts[4:8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])),
+                "sm_max_mhz": float(max(r[1] for r in rows)),
+                "power_w_max": float(max(r[2] for r in rows)),
+                "samples": len(rows), "reasons": reasons}
+
+
+# ------------------------------------------------------------- CPU oracle --
+def cpu_rate(nel: int, lx: int, iters: int, threads: int):
+    """GDOF*iter/s of the oracle's cg (OpenMP over elements) on nel^3 x lx."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_lib as O
+    ctx = O.Ctx(nel, nel, nel, lx, mask_mode=1, nthreads=threads, fma=False)
+    g = ctx.setup_g()
+    c = ctx.set_multiplicity()
+    f = ctx.set_f(c)
+    ctx.maskit(f)
+    work = tuple(np.zeros(ctx.n) for _ in range(5))
+    t0 = time.perf_counter()
+    ctx.cg(f, g, c, iters, work=work)
+    dt = time.perf_counter() - t0
+    return ctx.n * iters / dt / 1e9, dt, ctx.n
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    nel, iters = a.cpu_sample_nel, a.cpu_sample_iters
+    for _ in range(a.warmup):
+        cpu_rate(nel, a.lx, 1, threads)
+    rates, times = [], []
+    t_all = time.perf_counter()
+    for _ in range(a.steps):
+        r, dt, n = cpu_rate(nel, a.lx, iters, threads)
+        rates.append(r)
+        times.append(dt)
+    wall = time.perf_counter() - t_all
+    v = float(np.median(rates))
+    sample = f"{nel}^3 elements, lx1={a.lx} (n={n}), {iters} CG iterations per step"
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+            "warmup": a.warmup, "ms_per_step": float(np.median(times)) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"cg, {a.nel}^3 elements, lx1={a.lx}, {a.niter} iterations",
+                       "sample": sample, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------- GPU arm --
+def run_ours(a, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    import nekbone_gb300 as nb
+
+    nel, lx, niter = a.nel, a.lx, a.niter
+    t0 = time.perf_counter()
+    mesh = nb.DeviceMesh(nel, nel, nel, lx, mask_mode=1)
+    setup_s = time.perf_counter() - t0
+    n = mesh.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    mesh.setup_g(g.data_ptr())
+    mesh.set_multiplicity(c.data_ptr())
+    mesh.rhs_uniform(f.data_ptr(), c.data_ptr(), 20260 + rank)
+    x, r, w, p, z = (torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(5))
+    ptrs = [t.data_ptr() for t in (x, f, g, c, r, w, p, z)]
+    stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
+    torch.cuda.synchronize()
+
+    def step():
+        mesh.cg(*ptrs, niter)
+
+    for _ in range(a.warmup):
+        step()
+    nb.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(a.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    nb.sync()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    clocks = clk.summary()
+    ms_per_step = ms / a.steps
+    value = world * n * niter * a.steps / (ms / 1e3) / 1e9
+    launches_per_step = 2 + 3 * niter  # copy/mask/glsc3 + 3 kernels per iteration
+
+    # dominant kernel timing (the fused element operator) on the same stream
+    kms = mesh.time_cg_kernels(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
+                               r.data_ptr(), w.data_ptr(), p.data_ptr(), reps=10)
+    ax_bytes = 64 * n   # u 8 + g 48 + w 8 per point (ax, stored metric)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = ax_bytes / (kms[0] * 1e-3) / 1e9
+    flops_pt = 19 + 12 * lx
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "kernel": "k_ax<double,12,1> (fused element operator)",
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
+                "kernel_ms": {"ax": kms[0], "gs_fin": kms[1], "update": kms[2]},
+                "fp64_tflops": flops_pt * n / (kms[0] * 1e-3) / 1e12}
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+           "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"cg, {nel}^3 elements, lx1={lx}, {niter} FP64 iterations per step",
+                      "n": n, "mask": "full Dirichlet", "rhs": "seeded uniform[-1,1] per global DOF",
+                      "l2": "inputs larger than L2 (453 MB per vector)", "setup_s": setup_s},
+           "gpu_launches": launches_per_step * a.steps, "clocks": clocks, "roofline": roofline}
+
+    # ---- mixed vs FP64 time to tolerance
+    if not a.no_mixed:
+        xt = torch.zeros(n, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it64, rr64 = mesh.cg_tol(xt.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol,
+                                 max_iter=20000, check_every=50)
+        t64 = time.perf_counter() - t0
+        xm = torch.zeros(n, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outer, inner, rrm = mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
+                                          a.tol, 20, 5000)
+        tm = time.perf_counter() - t0
+        diff = float((xm - xt).abs().max().item() / max(xt.abs().max().item(), 1e-300))
+        out["mixed"] = {"tol": a.tol, "fp64_s": t64, "fp64_iters": it64, "fp64_relres": rr64,
+                        "mixed_s": tm, "mixed_outer": outer, "mixed_inner_iters": inner,
+                        "mixed_relres": rrm, "speedup": t64 / tm, "x_rel_diff": diff}
+        del xt, xm
+
+    # ---- end to end through the drop-in cg_ with pinned host buffers
+    if not a.no_e2e:
+        del x, r, w, p, z
+        torch.cuda.empty_cache()
+        hb = nb.Nekbone(nel, nel, nel, lx, mask_mode=1)
+        pin = lambda t: t.cpu().pin_memory()
+        fh, gh, ch = pin(f), pin(g), pin(c)
+        work = [torch.zeros(n, dtype=torch.float64).pin_memory() for _ in range(5)]
+        fn, gn, cn = fh.numpy(), gh.numpy(), ch.numpy()
+        wn = tuple(t.numpy() for t in work)
+        hb.cg(fn, gn, cn, niter, 0.0, wn)      # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            hb.cg(fn, gn, cn, niter, 0.0, wn)
+        e2e_s = (time.perf_counter() - t0) / a.steps
+        out["e2e"] = {"value": world * n * niter / e2e_s / 1e9, "unit": UNIT,
+                      "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 40 * n,
+                      "ms_per_step": e2e_s * 1e3, "call": "cg_ (C ABI, host arrays)"}
+
+    if rank == 0 and world == 1 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        v, dt, ns = cpu_rate(a.cpu_sample_nel, lx, a.cpu_sample_iters, threads)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{a.cpu_sample_nel}^3 elements, lx1={lx} (n={ns}), "
+                                         f"{a.cpu_sample_iters} FP64 CG iterations, {dt:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+        return
+    run_ours(a, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

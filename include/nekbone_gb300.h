@@ -1,0 +1,204 @@
+/*
+ * nekbone_gb300.h -- C ABI of the GB300 implementation of Nekbone's
+ * spectral-element Poisson CG hot path.
+ *
+ * Two layers:
+ *
+ *  1. Drop-in entry points with the reference's Fortran calling convention
+ *     (lower case, trailing underscore, every argument by reference, REAL =
+ *     double, INTEGER = int32_t, global ids int64_t).  They take HOST arrays,
+ *     exactly as the Fortran driver passes them, move them to the GPU, run the
+ *     CUDA kernels and copy the results back.  Each declaration cites the
+ *     reference routine it replaces (file:line in the reference project).
+ *     Routines that read Fortran common blocks in the reference read the
+ *     values published by nekbone_common_ here.
+ *
+ *  2. A device-resident API (nb_*) for callers that keep their vectors on the
+ *     GPU: mesh construction, ax, gather-scatter and the CG solvers on device
+ *     pointers, with no host round trip inside a solve.
+ *
+ * Errors: every call records a status (0 = ok).  In the default error mode
+ * (0) a failing call prints its message and exits the process with status 1,
+ * as the reference's jl fail() does (jl/fail.c:11-52).  In mode 1 the call
+ * returns and the status is read with nekbone_last_status().
+ */
+#ifndef NEKBONE_GB300_H
+#define NEKBONE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ status -- */
+int         nekbone_last_status(void);
+const char *nekbone_last_message(void);
+void        nekbone_clear_status(void);
+/* 0 = reference behaviour (print, exit(1)); 1 = record and return */
+void        nekbone_set_error_mode(int mode);
+int         nekbone_version(void);
+
+/* ------------------------------------------- common-block publication -- */
+/* The Fortran routines below read /dimn/ (SIZE), /hcglb/ lglel (PARALLEL),
+ * /dxyz/ dxm1 (DXYZ) and /comm_handles/ gsh (PARALLEL) instead of taking
+ * them as arguments.  The Fortran side publishes them once per mesh, after
+ * init_mesh, proxy_setupds and proxy_setup (driver.f:43-47). */
+void nekbone_common_(const int *nelx, const int *nely, const int *nelz,
+                     const int *nelt, const int *nx1, const int *lglel,
+                     const double *dxm1, const int *gsh);
+/* init_mesh's "cmask(-1) = 1.0" (driver.f:125): the next maskit rebuilds
+ * its index list (cg.f:231-254). */
+void nekbone_mask_reset_(void);
+/* 0 = the reference's maskit (list of element 1's Dirichlet points after the
+ * first call, cg.f:224-229); 1 = every element's Dirichlet faces. */
+void nekbone_set_mask_mode_(const int *mode);
+/* .true. selects h1mg_solve as solveM (MGRID build, cg.f:86-94,
+ * hsmg.f:960); .false. the copy of hsmg_dum.f:9-14. */
+void nekbone_set_mgrid_(const int *ifmgrid);
+/* /cflops/ flop_a, flop_cg (INPUT:8), accumulated as the reference does */
+void nekbone_get_flops_(double *flop_a, double *flop_cg);
+void nekbone_set_flops_(const double *flop_a, const double *flop_cg);
+
+/* --------------------------------------- jl gather-scatter (jl/gs.c) -- */
+/* gs_setup_ (jl/gs.c:1160-1170).  comm/np are accepted for signature
+ * compatibility; one process (np == 1) is supported. */
+void gs_setup_(int *handle, const int64_t *glo_num, const int *n,
+               const int *comm, const int *np);
+/* gs_op_ (jl/gs.c:1188-1193): dom 1 double, 2 float, 3 int, 4 long (64-bit);
+ * op 1 add, 2 mul, 3 min, 4 max; transpose != 0 swaps gather/scatter maps. */
+void gs_op_(const int *handle, void *u, const int *dom, const int *op,
+            const int *transpose);
+/* gs_free_ (jl/gs.c:1237-1242); handles are not reused */
+void gs_free_(const int *handle);
+/* dssum (prox_dssum.f:2-12): gs_op(gsh, f, 1, 1, 0) on the published gsh */
+void dssum_(double *f);
+
+/* -------------------------------------------------------- math.f / mxm -- */
+/* glsc3 (math.f:603-617): sum a*b*mult */
+double glsc3_(const double *a, const double *b, const double *mult,
+              const int *n);
+/* add2s1 (math.f:534-541): a = c1*a + b */
+void add2s1_(double *a, const double *b, const double *c1, const int *n);
+/* add2s2 (math.f:544-551): a = a + c1*b */
+void add2s2_(double *a, const double *b, const double *c1, const int *n);
+/* mxm (mxm_wrapper.f:1-52): c(n1,n3) = a(n1,n2) b(n2,n3) */
+void mxm_(const double *a, const int *n1, const double *b, const int *n2,
+          double *c, const int *n3);
+
+/* ---------------------------------------------------------------- cg.f -- */
+/* cg (cg.f:2-84): niter CG iterations on A = mask(QQ^T A_L + 0.1 I) */
+void cg_(double *x, const double *f, const double *g, const double *c,
+         double *r, double *w, double *p, double *z, const int *n,
+         const int *niter, double *flop_cg);
+/* ax (cg.f:96-125): w = mask(QQ^T A_L u + 0.1 u); ur..wk are scratch */
+void ax_(double *w, const double *u, const double *gxyz, double *ur,
+         double *us, double *ut, double *wk, const int *n);
+/* ax_e (cg.f:142-168): one element, w = A_L u */
+void ax_e_(double *w, const double *u, const double *g, double *ur,
+           double *us, double *ut, double *wk);
+/* local_grad3 (cg.f:170-187) */
+void local_grad3_(double *ur, double *us, double *ut, const double *u,
+                  const int *n, const double *D, const double *Dt);
+/* local_grad3_t (cg.f:189-212) */
+void local_grad3_t_(double *u, const double *ur, const double *us,
+                    const double *ut, const int *N, const double *D,
+                    const double *Dt, double *w);
+/* maskit (cg.f:214-258); pmask[0] is pmask(-1), pmask[1] is pmask(0) */
+void maskit_(double *w, double *pmask, const int *nx, const int *ny,
+             const int *nz);
+/* solveM (cg.f:86-94) */
+void solvem_(double *z, const double *r, const int *n);
+
+/* -------------------------------------------------------------- hsmg.f -- */
+/* h1mg_setup (hsmg.f:3-29) on the published mesh */
+void h1mg_setup_(void);
+/* h1mg_solve (hsmg.f:960-1034); like the reference it masks rhs in place */
+void h1mg_solve_(double *z, double *rhs, const int *nn);
+
+/* ------------------------------------- set-up routines on the hot path -- */
+/* zwgll (speclib.f:107-122) */
+void zwgll_(double *z, double *w, const int *np);
+/* semhat (semhat.f:2-37); w is scratch of 2n+2 */
+void semhat_(double *a, double *b, double *c, double *d, double *z,
+             double *w, const int *n);
+/* set_vert_box (prox_dssum.f:42-73) on the published mesh */
+void set_vert_box_(int64_t *glo_num, const int *nx);
+/* cubic (driver.f:196-247) */
+void cubic_(int *mx, int *my, int *mz, const int *np);
+/* setup_g (prox_setup.f:27-52) on the published mesh */
+void setup_g_(double *g);
+/* set_multiplicity (driver.f:274-291) on the published gsh */
+void set_multiplicity_(double *c);
+/* set_f (driver.f:88-101) */
+void set_f_(double *f, const double *c, const int *n);
+
+/* ------------------------------------------ device-resident API (nb_*) -- */
+typedef struct nb_mesh nb_mesh;
+
+/* Box mesh nelx*nely*nelz, lx1 points per direction, brick element order
+ * and numbering of the reference (driver.f:117-194, prox_dssum.f:42-73).
+ * mask_mode 1 = Dirichlet on every outer face. */
+int  nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
+                    int mask_mode);
+int  nb_mesh_destroy(nb_mesh *mesh);
+long nb_mesh_npts(const nb_mesh *mesh);
+int  nb_mesh_info(const nb_mesh *mesh, int *nelt, int *lx1, int *fused);
+
+/* Device vectors (all pointers below are device pointers of length n, or 6n
+ * for g).  g = setup_g form; c = inverse multiplicity; f = seeded uniform
+ * [-1,1] per global point, dssum'd, times c, masked. */
+int nb_setup_g(nb_mesh *mesh, double *g);
+int nb_set_multiplicity(nb_mesh *mesh, double *c);
+int nb_rhs_uniform(nb_mesh *mesh, double *f, const double *c, uint64_t seed);
+
+/* w = A u on the device (FP64) */
+int nb_ax(nb_mesh *mesh, double *w, const double *u, const double *g);
+/* dssum on a device vector (dom 1 double, 2 float) */
+int nb_dssum(nb_mesh *mesh, void *u, int dom);
+
+/* Plain FP64 CG, niter iterations (cg.f:2-84), device pointers.  hist
+ * (host, may be NULL) receives 5*(niter+1) values per iteration: rnorm,
+ * alpha, beta, pap, rtz1.  flags bit0: force the unfused path; bit1: use
+ * the hsmg preconditioner (nb_mg_setup first). */
+int nb_cg(nb_mesh *mesh, double *x, const double *f, const double *g,
+          const double *c, double *r, double *w, double *p, double *z,
+          int niter, int flags, double *hist);
+
+/* FP32 CG on device float vectors (the inner solver of the mixed path) */
+int nb_cg_f32(nb_mesh *mesh, float *x, const float *f, const float *g,
+              const float *c, float *r, float *w, float *p, int niter,
+              double *hist);
+
+/* Mixed precision: FP32 inner CG (inner_iters per correction) inside an
+ * FP64 defect-correction loop until sqrt(r'Cr)/sqrt(r0'Cr0) <= tol or
+ * max_outer corrections.  Returns outer steps in *outer, inner iterations
+ * in *inner_total and the final relative residual in *relres. */
+int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
+                const double *c, double tol, int inner_iters, int max_outer,
+                int *outer, int *inner_total, double *relres);
+
+/* FP64 CG until sqrt(r'Cr)/sqrt(r0'Cr0) <= tol (max_iter cap); checks the
+ * residual every check_every iterations. */
+int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
+              const double *c, double tol, int max_iter, int check_every,
+              int *iters, double *relres);
+
+/* Synchronise the library's stream. */
+int nb_sync(void);
+/* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for
+ * callers that record events or order their own work against the library. */
+void *nb_stream(void);
+/* Average device time (ms) of each kernel of one fused FP64 CG iteration --
+ * [0] element operator + direction update, [1] boundary gather-scatter and
+ * pap, [2] x/r update and rtr -- over reps iterations, timed with CUDA
+ * events on the library stream.  Vectors as for nb_cg; x and r are
+ * overwritten. */
+int nb_time_cg_kernels(nb_mesh *mesh, double *x, const double *f,
+                       const double *g, const double *c, double *r, double *w,
+                       double *p, int reps, double *ms3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,401 @@
+"""nekbone_gb300 -- GB300 (sm_103a) implementation of Nekbone's spectral-element
+Poisson CG hot path behind the reference's own routine interface.
+
+The native library ``libnekbone_gb300.so`` (CUDA kernels + C ABI, see
+``include/nekbone_gb300.h``) does all the work.  This module is the host-side
+mirror of the reference's Fortran-callable routines -- same names, argument
+meaning and error behaviour -- for callers that drive the hot path from
+Python, and a thin wrapper of the device-resident ``nb_*`` API.
+
+There is no fallback: importing the package loads the native library and
+raises ``ImportError`` when it has not been built
+(``python -m nekbone_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes as _C
+from pathlib import Path as _Path
+
+import numpy as _np
+
+_LIB_PATH = _path = _Path(__file__).resolve().parent / "libnekbone_gb300.so"
+
+if not _LIB_PATH.exists():
+    raise ImportError(
+        f"nekbone_gb300 native library missing at {_LIB_PATH}; build it with "
+        "'python -m nekbone_gb300.build' (requires nvcc)")
+
+lib = _C.CDLL(str(_LIB_PATH))
+
+_i = _C.c_int
+_l = _C.c_long
+_d = _C.c_double
+_p = _C.c_void_p
+_ip = _C.POINTER(_C.c_int)
+_dp = _C.POINTER(_C.c_double)
+
+#: every symbol include/nekbone_gb300.h declares
+EXPORTS = (
+    "nekbone_last_status", "nekbone_last_message", "nekbone_clear_status",
+    "nekbone_set_error_mode", "nekbone_version", "nekbone_common_",
+    "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
+    "nekbone_get_flops_", "nekbone_set_flops_", "gs_setup_", "gs_op_",
+    "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
+    "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
+    "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
+    "cubic_", "setup_g_", "set_multiplicity_", "set_f_", "nb_mesh_create",
+    "nb_mesh_destroy", "nb_mesh_npts", "nb_mesh_info", "nb_setup_g",
+    "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
+    "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync", "nb_stream",
+    "nb_time_cg_kernels",
+)
+
+lib.nekbone_last_status.restype = _i
+lib.nekbone_last_message.restype = _C.c_char_p
+lib.glsc3_.restype = _d
+lib.nb_mesh_npts.restype = _l
+for _name in ("nb_mesh_create", "nb_mesh_destroy", "nb_mesh_info", "nb_setup_g",
+              "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
+              "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync"):
+    getattr(lib, _name).restype = _i
+lib.nb_mesh_npts.argtypes = [_p]
+lib.nb_mesh_destroy.argtypes = [_p]
+lib.nb_rhs_uniform.argtypes = [_p, _p, _p, _C.c_uint64]
+lib.nb_cg.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _p, _i, _i, _p]
+lib.nb_cg_f32.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
+lib.nb_cg_mixed.argtypes = [_p, _p, _p, _p, _p, _d, _i, _i, _p, _p, _p]
+lib.nb_cg_tol.argtypes = [_p, _p, _p, _p, _p, _d, _i, _i, _p, _p]
+lib.nb_ax.argtypes = [_p, _p, _p, _p]
+lib.nb_dssum.argtypes = [_p, _p, _i]
+lib.nb_setup_g.argtypes = [_p, _p]
+lib.nb_set_multiplicity.argtypes = [_p, _p]
+lib.nb_mesh_info.argtypes = [_p, _p, _p, _p]
+lib.nb_stream.restype = _p
+lib.nb_time_cg_kernels.restype = _i
+lib.nb_time_cg_kernels.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
+
+# return-status error mode for Python callers: errors raise NekboneError
+lib.nekbone_set_error_mode(1)
+
+
+class NekboneError(RuntimeError):
+    """A failed library call; ``status`` is the library's status code."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"[status {status}] {message}")
+        self.status = status
+
+
+def _check(ret: int | None = None) -> None:
+    st = lib.nekbone_last_status() if ret is None else ret
+    if st:
+        msg = lib.nekbone_last_message().decode(errors="replace")
+        lib.nekbone_clear_status()
+        raise NekboneError(st, msg)
+
+
+def _ref(v, t=_C.c_int):
+    return _C.byref(t(v))
+
+
+def _ptr(a: _np.ndarray):
+    return a.ctypes.data_as(_p)
+
+
+def _f64(a) -> _np.ndarray:
+    a = _np.asarray(a)
+    if a.dtype != _np.float64 or not a.flags.c_contiguous:
+        raise TypeError("expected a C-contiguous float64 array")
+    return a
+
+
+# ------------------------------------------------------------ set-up path --
+def zwgll(np_: int):
+    """GLL points and weights (speclib.f ZWGLL)."""
+    z = _np.zeros(np_)
+    w = _np.zeros(np_)
+    lib.zwgll_(_ptr(z), _ptr(w), _ref(np_))
+    return z, w
+
+
+def semhat(n: int):
+    """1-D matrices of degree n (semhat.f): a, b, c, d, z (d column-major)."""
+    np_ = n + 1
+    a, c, d = (_np.zeros(np_ * np_) for _ in range(3))
+    b, z, w = _np.zeros(np_), _np.zeros(np_), _np.zeros(2 * np_)
+    lib.semhat_(_ptr(a), _ptr(b), _ptr(c), _ptr(d), _ptr(z), _ptr(w), _ref(n))
+    return a, b, c, d, z
+
+
+def cubic(np_: int):
+    """Most cube-like factorisation np = mx*my*mz (driver.f cubic)."""
+    mx, my, mz = _C.c_int(), _C.c_int(), _C.c_int()
+    lib.cubic_(_C.byref(mx), _C.byref(my), _C.byref(mz), _ref(np_))
+    return mx.value, my.value, mz.value
+
+
+# ----------------------------------------------------------- gather-scatter --
+_DOM = {_np.dtype(_np.float64): 1, _np.dtype(_np.float32): 2,
+        _np.dtype(_np.int32): 3, _np.dtype(_np.int64): 4}
+
+
+def gs_setup(glo_num) -> int:
+    """gs_setup (jl/gs.c:1160): handle for the global numbering glo_num."""
+    ids = _np.ascontiguousarray(glo_num, dtype=_np.int64)
+    h = _C.c_int(-1)
+    lib.gs_setup_(_C.byref(h), _ptr(ids), _ref(len(ids)), _ref(0), _ref(1))
+    _check()
+    return h.value
+
+
+def gs_op(handle: int, u: _np.ndarray, op: int = 1, transpose: int = 0) -> None:
+    """gs_op (jl/gs.c:1188) in place; the dom follows u's dtype."""
+    dom = _DOM.get(u.dtype)
+    if dom is None or not u.flags.c_contiguous:
+        raise TypeError("u must be a C-contiguous float64/float32/int32/int64 array")
+    lib.gs_op_(_ref(handle), _ptr(u), _ref(dom), _ref(op), _ref(transpose))
+    _check()
+
+
+def gs_free(handle: int) -> None:
+    lib.gs_free_(_ref(handle))
+    _check()
+
+
+# --------------------------------------------------------------- math.f --
+def glsc3(a, b, mult) -> float:
+    a, b, mult = _f64(a), _f64(b), _f64(mult)
+    v = lib.glsc3_(_ptr(a), _ptr(b), _ptr(mult), _ref(len(a)))
+    _check()
+    return v
+
+
+def add2s1(a, b, c1: float) -> None:
+    a, b = _f64(a), _f64(b)
+    lib.add2s1_(_ptr(a), _ptr(b), _ref(c1, _C.c_double), _ref(len(a)))
+    _check()
+
+
+def add2s2(a, b, c1: float) -> None:
+    a, b = _f64(a), _f64(b)
+    lib.add2s2_(_ptr(a), _ptr(b), _ref(c1, _C.c_double), _ref(len(a)))
+    _check()
+
+
+def mxm(a, n1: int, b, n2: int, n3: int) -> _np.ndarray:
+    a, b = _f64(a), _f64(b)
+    c = _np.zeros(n1 * n3)
+    lib.mxm_(_ptr(a), _ref(n1), _ptr(b), _ref(n2), _ptr(c), _ref(n3))
+    _check()
+    return c
+
+
+def local_grad3(u, n: int, D, Dt):
+    m3 = (n + 1) ** 3
+    ur, us, ut = _np.zeros(m3), _np.zeros(m3), _np.zeros(m3)
+    lib.local_grad3_(_ptr(ur), _ptr(us), _ptr(ut), _ptr(_f64(u)), _ref(n),
+                     _ptr(_f64(D)), _ptr(_f64(Dt)))
+    _check()
+    return ur, us, ut
+
+
+def local_grad3_t(ur, us, ut, n: int, D, Dt):
+    m3 = (n + 1) ** 3
+    u, w = _np.zeros(m3), _np.zeros(m3)
+    lib.local_grad3_t_(_ptr(u), _ptr(_f64(ur)), _ptr(_f64(us)), _ptr(_f64(ut)),
+                       _ref(n), _ptr(_f64(D)), _ptr(_f64(Dt)), _ptr(w))
+    _check()
+    return u, w
+
+
+# ------------------------------------------------------------ driver level --
+class Nekbone:
+    """The Fortran driver's view of one mesh (driver.f:38-67): publishes the
+    common blocks and calls the drop-in routines with host arrays.
+
+    mask_mode 0 reproduces the reference's maskit (after the first call only
+    element 1's Dirichlet points are zeroed, cg.f:224-229); 1 masks every
+    element's outer faces.
+    """
+
+    def __init__(self, nelx: int, nely: int, nelz: int, nx1: int,
+                 mask_mode: int = 0, lglel=None):
+        self.nelx, self.nely, self.nelz, self.nx1 = nelx, nely, nelz, nx1
+        self.nelt = nelx * nely * nelz
+        self.n = self.nelt * nx1 ** 3
+        self.lglel = (_np.arange(1, self.nelt + 1, dtype=_np.int32) if lglel is None
+                      else _np.ascontiguousarray(lglel, dtype=_np.int32))
+        _, _, _, d, z = semhat(nx1 - 1)
+        self.dxm1 = d
+        lib.nekbone_set_mask_mode_(_ref(mask_mode))
+        _check()
+        # publish /dimn/ and /hcglb/ so set_vert_box can run, then gs_setup
+        lib.nekbone_common_(_ref(nelx), _ref(nely), _ref(nelz), _ref(self.nelt),
+                            _ref(nx1), _ptr(self.lglel), _ptr(self.dxm1), _ref(-1))
+        _check()
+        self.glo_num = _np.zeros(self.n, dtype=_np.int64)
+        lib.set_vert_box_(_ptr(self.glo_num), _ref(nx1))
+        _check()
+        self.gsh = gs_setup(self.glo_num)
+        lib.nekbone_common_(_ref(nelx), _ref(nely), _ref(nelz), _ref(self.nelt),
+                            _ref(nx1), _ptr(self.lglel), _ptr(self.dxm1), _ref(self.gsh))
+        _check()
+
+    def set_multiplicity(self) -> _np.ndarray:
+        c = _np.zeros(self.n)
+        lib.set_multiplicity_(_ptr(c))
+        _check()
+        return c
+
+    def setup_g(self) -> _np.ndarray:
+        g = _np.zeros(6 * self.n)
+        lib.setup_g_(_ptr(g))
+        _check()
+        return g
+
+    def set_f(self, c) -> _np.ndarray:
+        f = _np.zeros(self.n)
+        lib.set_f_(_ptr(f), _ptr(_f64(c)), _ref(self.n))
+        _check()
+        return f
+
+    def dssum(self, f) -> None:
+        lib.dssum_(_ptr(_f64(f)))
+        _check()
+
+    def mask_reset(self) -> None:
+        lib.nekbone_mask_reset_()
+
+    def set_mgrid(self, on: bool) -> None:
+        lib.nekbone_set_mgrid_(_ref(1 if on else 0))
+
+    def h1mg_setup(self) -> None:
+        lib.h1mg_setup_()
+        _check()
+
+    def h1mg_solve(self, rhs) -> _np.ndarray:
+        z = _np.zeros(self.n)
+        lib.h1mg_solve_(_ptr(z), _ptr(_f64(rhs)), _ref(self.n))
+        _check()
+        return z
+
+    def ax(self, u, g) -> _np.ndarray:
+        w = _np.zeros(self.n)
+        s = _np.zeros(1)
+        lib.ax_(_ptr(w), _ptr(_f64(u)), _ptr(_f64(g)), _ptr(s), _ptr(s), _ptr(s), _ptr(s),
+                _ref(self.n))
+        _check()
+        return w
+
+    def ax_e(self, u, g) -> _np.ndarray:
+        m3 = self.nx1 ** 3
+        w, s = _np.zeros(m3), _np.zeros(1)
+        lib.ax_e_(_ptr(w), _ptr(_f64(u)), _ptr(_f64(g)), _ptr(s), _ptr(s), _ptr(s), _ptr(s))
+        _check()
+        return w
+
+    def maskit(self, w, pmask) -> None:
+        lib.maskit_(_ptr(_f64(w)), _ptr(_f64(pmask)), _ref(self.nx1), _ref(self.nx1),
+                    _ref(self.nx1))
+        _check()
+
+    def cg(self, f, g, c, niter: int, flop_cg: float = 0.0, work=None):
+        """cg (cg.f:2-84).  Returns x, r, w, p, z, flop_cg."""
+        n = self.n
+        x, r, w, p, z = work if work is not None else tuple(_np.zeros(n) for _ in range(5))
+        fc = _C.c_double(flop_cg)
+        lib.cg_(_ptr(x), _ptr(_f64(f)), _ptr(_f64(g)), _ptr(_f64(c)), _ptr(r), _ptr(w),
+                _ptr(p), _ptr(z), _ref(n), _ref(niter), _C.byref(fc))
+        _check()
+        return x, r, w, p, z, fc.value
+
+    @staticmethod
+    def flops():
+        a, c = _C.c_double(), _C.c_double()
+        lib.nekbone_get_flops_(_C.byref(a), _C.byref(c))
+        return a.value, c.value
+
+    @staticmethod
+    def set_flops(a: float, c: float) -> None:
+        lib.nekbone_set_flops_(_ref(a, _C.c_double), _ref(c, _C.c_double))
+
+
+# ------------------------------------------------------------ device API --
+class DeviceMesh:
+    """Box mesh resident on the GPU (the nb_* API).  Vectors are passed as
+    raw device pointers (ints), e.g. ``torch.Tensor.data_ptr()``."""
+
+    def __init__(self, nelx: int, nely: int, nelz: int, lx1: int, mask_mode: int = 1):
+        h = _p()
+        _check(lib.nb_mesh_create(_C.byref(h), nelx, nely, nelz, lx1, mask_mode))
+        self._h = h
+        self.n = int(lib.nb_mesh_npts(h))
+        nelt, lx, fused = _C.c_int(), _C.c_int(), _C.c_int()
+        _check(lib.nb_mesh_info(h, _C.byref(nelt), _C.byref(lx), _C.byref(fused)))
+        self.nelt, self.lx1, self.fused = nelt.value, lx.value, bool(fused.value)
+        self.dims = (nelx, nely, nelz)
+
+    def close(self) -> None:
+        if self._h:
+            lib.nb_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup_g(self, g_ptr: int) -> None:
+        _check(lib.nb_setup_g(self._h, _p(g_ptr)))
+
+    def set_multiplicity(self, c_ptr: int) -> None:
+        _check(lib.nb_set_multiplicity(self._h, _p(c_ptr)))
+
+    def rhs_uniform(self, f_ptr: int, c_ptr: int, seed: int) -> None:
+        _check(lib.nb_rhs_uniform(self._h, _p(f_ptr), _p(c_ptr), seed))
+
+    def ax(self, w_ptr: int, u_ptr: int, g_ptr: int) -> None:
+        _check(lib.nb_ax(self._h, _p(w_ptr), _p(u_ptr), _p(g_ptr)))
+
+    def dssum(self, u_ptr: int, dom: int = 1) -> None:
+        _check(lib.nb_dssum(self._h, _p(u_ptr), dom))
+
+    def cg(self, x, f, g, c, r, w, p, z, niter: int, flags: int = 0, hist: bool = False):
+        h = _np.zeros(5 * (niter + 1)) if hist else None
+        _check(lib.nb_cg(self._h, _p(x), _p(f), _p(g), _p(c), _p(r), _p(w), _p(p), _p(z),
+                         niter, flags, _ptr(h) if hist else None))
+        return h.reshape(niter + 1, 5) if hist else None
+
+    def cg_f32(self, x, f, g, c, r, w, p, niter: int, hist: bool = False):
+        h = _np.zeros(5 * (niter + 1)) if hist else None
+        _check(lib.nb_cg_f32(self._h, _p(x), _p(f), _p(g), _p(c), _p(r), _p(w), _p(p),
+                             niter, _ptr(h) if hist else None))
+        return h.reshape(niter + 1, 5) if hist else None
+
+    def cg_mixed(self, x, f, g, c, tol: float, inner_iters: int = 20, max_outer: int = 500):
+        o, it, rr = _C.c_int(), _C.c_int(), _C.c_double()
+        _check(lib.nb_cg_mixed(self._h, _p(x), _p(f), _p(g), _p(c), tol, inner_iters,
+                               max_outer, _C.byref(o), _C.byref(it), _C.byref(rr)))
+        return o.value, it.value, rr.value
+
+    def time_cg_kernels(self, x, f, g, c, r, w, p, reps: int = 10):
+        ms = _np.zeros(3)
+        _check(lib.nb_time_cg_kernels(self._h, _p(x), _p(f), _p(g), _p(c), _p(r), _p(w),
+                                      _p(p), reps, _ptr(ms)))
+        return ms
+
+    def cg_tol(self, x, f, g, c, tol: float, max_iter: int = 20000, check_every: int = 25):
+        it, rr = _C.c_int(), _C.c_double()
+        _check(lib.nb_cg_tol(self._h, _p(x), _p(f), _p(g), _p(c), tol, max_iter,
+                             check_every, _C.byref(it), _C.byref(rr)))
+        return it.value, rr.value
+
+
+def stream_handle() -> int:
+    """cudaStream_t of the library (wrap with torch.cuda.ExternalStream)."""
+    return int(lib.nb_stream() or 0)
+
+
+def sync() -> None:
+    _check(lib.nb_sync())

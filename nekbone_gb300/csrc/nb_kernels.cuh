@@ -1,0 +1,357 @@
+// nb_kernels.cuh -- device kernels of the Nekbone CG hot path.
+//
+// ax_e (cg.f:142-168) is evaluated one element per CTA with an (lx1 x lx1)
+// thread tile: thread (i,j) owns the column (i,j,0..lx1-1).  The element is
+// staged in shared memory; the t-direction contractions use the thread's own
+// column held in registers.  Every contraction is the reference's
+// left-to-right sum (mxfN, mxm_std.f:255) written as an explicit product
+// followed by a fused multiply-add chain, so the FP64 result equals the
+// oracle's fma variant bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nb {
+
+// ----------------------------------------------------------- arithmetic --
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { typedef double2 type; };
+template <> struct Vec2<float> { typedef float2 type; };
+
+// ------------------------------------------------------------ reduction --
+// Deterministic block sum of one value per thread: a fixed shuffle tree in
+// the accumulation type A (float for the FP32 kernels, which keeps FP64
+// instructions off the per-point path), then the per-warp results summed in
+// FP64 in a fixed order.  Result valid in thread 0.
+template <typename A>
+__device__ __forceinline__ double block_sum(A v, double *sh) {
+  const int lane = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nt = blockDim.x * blockDim.y;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = lane >> 5, nw = (nt + 31) >> 5;
+  __syncthreads();
+  if ((lane & 31) == 0) sh[w] = double(v);
+  __syncthreads();
+  double s = 0.0;
+  if (lane == 0)
+    for (int q = 0; q < nw; ++q) s += sh[q];
+  return s;
+}
+
+// Sum of partial[0..n) in a fixed order by one block (result in thread 0).
+__device__ __forceinline__ double block_sum_array(const double *partial, int n,
+                                                  double *sh) {
+  const int t = threadIdx.x + threadIdx.y * blockDim.x;
+  const int nt = blockDim.x * blockDim.y;
+  double v = 0.0;
+  for (int q = t; q < n; q += nt) v += partial[q];
+  return block_sum<double>(v, sh);
+}
+
+// Returns true in the block that finished last (all threads), after its
+// partial is visible.  counter is reset for the next launch.
+__device__ __forceinline__ bool last_block(unsigned *counter, int nblocks) {
+  __shared__ bool amlast;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    const unsigned prev = atomicAdd(counter, 1u);
+    amlast = (prev == unsigned(nblocks) - 1u);
+    if (amlast) *counter = 0u;
+  }
+  __syncthreads();
+  if (amlast) __threadfence();
+  return amlast;
+}
+
+// CG scalars, device resident (cg.f:27-75 variables).
+struct CgScalars {
+  double rtz1, rtz2, beta, pap, alpha, rtr, rnorm;
+  double rtr_first;  // rtr of iteration 1 (cg.f:68)
+  int iter;
+  int pad;
+};
+
+// ------------------------------------------------------------ ax kernel --
+// MODE 0: w = A_L u for every point (the element loop of ax, cg.f:111-114).
+// MODE 1: fused CG pass -- p = z + beta*p (p = z when first), stored; the
+//         element product w_L = A_L p; interior points (not shared, never
+//         masked) are finished here: w = w_L + 0.1 p (ax, cg.f:119); element
+//         boundary points keep w_L for the gather-scatter pass; the interior
+//         part of pap = glsc3(w,c,p) goes to partial[blockIdx.x].
+template <typename T>
+struct AxArgs {
+  T *w;
+  const T *u;        // MODE 0 input; MODE 1: z
+  T *p;              // MODE 1: search direction (read old, write new)
+  const T *g;        // gxyz(6, nxyz, nelt)
+  const T *c;        // MODE 1: inverse multiplicity
+  const T *D;        // dxm1(lx1,lx1) column-major: D(i,m) at D[i + m*lx1]
+  const CgScalars *sc;
+  double *partial;
+  int first;         // MODE 1: first iteration (beta = 0)
+  int nelt;
+};
+
+template <typename T, int LX>
+struct AxShared {
+  T u[LX * LX * LX];
+  T wr[LX * LX * LX];
+  T ws[LX * LX * LX];
+  T Dp[LX * (LX + 1)];   // Dp[i*(LX+1)+m] = D(i,m)
+  T Dtp[LX * (LX + 1)];  // Dtp[i*(LX+1)+m] = D(m,i)
+  double red[32];
+};
+
+template <typename T, int LX, int MODE>
+__global__ void __launch_bounds__(LX * LX)
+    k_ax(AxArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  AxShared<T, LX> &sm = *reinterpret_cast<AxShared<T, LX> *>(smem_raw);
+  constexpr int L2 = LX * LX, L3 = LX * LX * LX, LP = LX + 1;
+  const int i = threadIdx.x, j = threadIdx.y;
+  const int tid = i + LX * j;
+  const int e = blockIdx.x;
+  const size_t base = size_t(e) * L3;
+
+  for (int q = tid; q < L2; q += L2) {
+    const int r = q % LX, m = q / LX;  // D(r,m)
+    const T d = a.D[r + m * LX];
+    sm.Dp[r * LP + m] = d;
+    sm.Dtp[m * LP + r] = d;
+  }
+
+  T ureg[LX];
+  T beta = T(0);
+  if (MODE == 1 && !a.first) beta = T(a.sc->beta);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + tid;
+    T v;
+    if (MODE == 1) {
+      const T z = a.u[id];
+      v = a.first ? z : fma_rn(beta, a.p[id], z);  // add2s1, math.f:534
+      a.p[id] = v;
+    } else {
+      v = a.u[id];
+    }
+    ureg[k] = v;
+    sm.u[k * L2 + tid] = v;
+  }
+  __syncthreads();
+
+  T wtreg[LX];
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    // local_grad3, cg.f:170-187
+    const T *urow = &sm.u[k * L2 + j * LX];
+    T ur = mul_rn(sm.Dp[i * LP + 0], urow[0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) ur = fma_rn(sm.Dp[i * LP + m], urow[m], ur);
+    const T *ucol = &sm.u[k * L2 + i];
+    T us = mul_rn(ucol[0], sm.Dp[j * LP + 0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) us = fma_rn(ucol[m * LX], sm.Dp[j * LP + m], us);
+    T ut = mul_rn(ureg[0], sm.Dp[k * LP + 0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) ut = fma_rn(ureg[m], sm.Dp[k * LP + m], ut);
+    // metric, cg.f:156-163
+    const size_t pt = base + size_t(k) * L2 + tid;
+    typedef typename Vec2<T>::type V2;
+    const V2 *gp = reinterpret_cast<const V2 *>(a.g + 6 * pt);
+    const V2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
+    T wr = mul_rn(g01.x, ur);
+    wr = fma_rn(g01.y, us, wr);
+    wr = fma_rn(g23.x, ut, wr);
+    T ws = mul_rn(g01.y, ur);
+    ws = fma_rn(g23.y, us, ws);
+    ws = fma_rn(g45.x, ut, ws);
+    T wt = mul_rn(g23.x, ur);
+    wt = fma_rn(g45.x, us, wt);
+    wt = fma_rn(g45.y, ut, wt);
+    sm.wr[k * L2 + tid] = wr;
+    sm.ws[k * L2 + tid] = ws;
+    wtreg[k] = wt;
+  }
+  __syncthreads();
+
+  T part = T(0);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    // local_grad3_t, cg.f:189-212: u = Dt*ur; w = us*D; u += w; w = ut*D; u += w
+    const T *rrow = &sm.wr[k * L2 + j * LX];
+    T tr = mul_rn(sm.Dtp[i * LP + 0], rrow[0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) tr = fma_rn(sm.Dtp[i * LP + m], rrow[m], tr);
+    const T *scol = &sm.ws[k * L2 + i];
+    T ts = mul_rn(scol[0], sm.Dtp[j * LP + 0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) ts = fma_rn(scol[m * LX], sm.Dtp[j * LP + m], ts);
+    T tt = mul_rn(wtreg[0], sm.Dtp[k * LP + 0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) tt = fma_rn(wtreg[m], sm.Dtp[k * LP + m], tt);
+    T wl = add_rn(add_rn(tr, ts), tt);
+    const size_t id = base + size_t(k) * L2 + tid;
+    if (MODE == 1) {
+      const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
+                            (k > 0) && (k < LX - 1);
+      if (interior) {
+        wl = fma_rn(T(0.1), ureg[k], wl);  // add2s2(w,u,.1,n), cg.f:119
+        part = fma_rn(mul_rn(wl, a.c[id]), ureg[k], part);
+      }
+    }
+    a.w[id] = wl;
+  }
+  if (MODE == 1) {
+    const double s = block_sum<T>(part, sm.red);
+    if (i == 0 && j == 0) a.partial[e] = s;
+  }
+}
+
+template <typename T, int LX>
+constexpr size_t ax_smem_bytes() {
+  return sizeof(AxShared<T, LX>);
+}
+
+// ------------------------------------------------ gather-scatter finish --
+// For every group of element-boundary points: t = sum of w_L over the group
+// in jl's member order (gather_T_add, jl/gs_local.c:60-75); each member gets
+// w = t + 0.1 p (cg.f:119) or 0 when masked (maskit, cg.f:214-258); the
+// boundary part of pap = glsc3(w,c,p) is reduced; the block that finishes
+// last adds the interior partials, forms pap and alpha = rtz1/pap (cg.f:59-61).
+// idx: member index in bits 0..30, mask flag in bit 31.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_gs_fin(T *__restrict__ w, const T *__restrict__ p,
+             const T *__restrict__ c, const int *__restrict__ off,
+             const unsigned *__restrict__ idx, int ng,
+             double *__restrict__ partial, const double *__restrict__ ax_partial,
+             int n_ax_partial, unsigned *counter, CgScalars *sc) {
+  __shared__ double red[32];
+  T part = T(0);
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng;
+       g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    T t = w[idx[b] & 0x7fffffffu];
+    for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
+    for (int q = b; q < e; ++q) {
+      const unsigned m = idx[q];
+      const unsigned id = m & 0x7fffffffu;
+      const T pv = p[id];
+      T v = fma_rn(T(0.1), pv, t);
+      if (m & 0x80000000u) v = T(0);
+      w[id] = v;
+      part = fma_rn(mul_rn(v, c[id]), pv, part);
+    }
+  }
+  const double s = block_sum<T>(part, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (last_block(counter, gridDim.x)) {
+    const double s1 = block_sum_array(ax_partial, n_ax_partial, red);
+    __syncthreads();
+    const double s2 = block_sum_array(partial, gridDim.x, red);
+    if (threadIdx.x == 0) {
+      const double pap = s1 + s2;
+      sc->pap = pap;
+      sc->alpha = sc->rtz1 / pap;
+    }
+  }
+}
+
+// ------------------------------------------------------------ CG update --
+// x += alpha p; r -= alpha w (add2s2, cg.f:63-64); rtr = glsc3(r,c,r) (cg.f:66).
+// The last block forms rnorm and, for the identity preconditioner (z = r),
+// the next rtz1 = rtr and beta = rtz1/rtz2 (cg.f:52-55).
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_cg_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                const T *__restrict__ w, const T *__restrict__ c, long n,
+                double *__restrict__ partial, unsigned *counter, CgScalars *sc,
+                double *hist, int iter, int identity_precond) {
+  __shared__ double red[32];
+  const T alpha = T(sc->alpha);
+  const T alphm = -alpha;
+  T part = T(0);
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    x[q] = fma_rn(alpha, p[q], x[q]);
+    const T rv = fma_rn(alphm, w[q], r[q]);
+    r[q] = rv;
+    part = fma_rn(mul_rn(rv, c[q]), rv, part);
+  }
+  const double s = block_sum<T>(part, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (last_block(counter, gridDim.x)) {
+    const double rtr = block_sum_array(partial, gridDim.x, red);
+    if (threadIdx.x == 0) {
+      sc->rtr = rtr;
+      if (iter == 1) sc->rtr_first = rtr;
+      sc->rnorm = sqrt(rtr);
+      sc->iter = iter;
+      if (hist) {
+        double *h = hist + 5 * iter;
+        h[0] = sc->rnorm;
+        h[1] = sc->alpha;
+        h[2] = sc->beta;
+        h[3] = sc->pap;
+        h[4] = sc->rtz1;
+      }
+      if (identity_precond) {
+        sc->rtz2 = sc->rtz1;
+        sc->rtz1 = rtr;
+        sc->beta = sc->rtz1 / sc->rtz2;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------ reductions --
+// s = glsc3(a,b,mult) (math.f:603-617) into *out via partials; optional
+// CG bookkeeping: mode 1 = initial rnorm (cg.f:42), mode 2 = rtz1 and beta of
+// a preconditioned iteration (cg.f:51-55).
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_glsc3(const T *__restrict__ a, const T *__restrict__ b,
+            const T *__restrict__ m, long n, double *__restrict__ partial,
+            unsigned *counter, double *out, CgScalars *sc, int mode,
+            double *hist, int iter) {
+  __shared__ double red[32];
+  T part = T(0);
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    part = fma_rn(mul_rn(a[q], b[q]), m[q], part);
+  const double s = block_sum<T>(part, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (last_block(counter, gridDim.x)) {
+    const double v = block_sum_array(partial, gridDim.x, red);
+    if (threadIdx.x == 0) {
+      if (out) *out = v;
+      if (sc && mode == 1) {
+        sc->rnorm = sqrt(v);
+        sc->rtz1 = v;   // with z = r the first rtz1 equals this value
+        sc->rtz2 = 1.0;
+        sc->beta = 0.0;
+        if (hist) {
+          hist[0] = sc->rnorm;
+          hist[1] = hist[2] = hist[3] = hist[4] = 0.0;
+        }
+      }
+      if (sc && mode == 2) {
+        sc->rtz2 = sc->rtz1;
+        sc->rtz1 = v;
+        sc->beta = (iter == 1) ? 0.0 : v / sc->rtz2;
+      }
+    }
+  }
+}
+
+}  // namespace nb

@@ -1,0 +1,705 @@
+// nb_mg.cu -- hybrid Schwarz multigrid preconditioner (hsmg.f) on the GPU.
+//
+// h1mg_solve (hsmg.f:960-1034) is an additive V-cycle: an overlapping
+// Schwarz smoother on every level but the coarsest, weighted restriction
+// down, a "coarse solve" that is a copy plus dssum (hsmg_coarse_solve,
+// hsmg.f:945-957), and interpolation back up with no post-smoothing.  The
+// Schwarz step (h1mg_schwarz_part1, hsmg.f:1053-1095) works on elements
+// extended by one ghost layer: ghost faces receive the neighbour's first
+// interior layer through a gather-scatter on the extended numbering, each
+// extended element is solved by fast diagonalisation (h1mg_do_fast,
+// hsmg.f:1297-1318), and the overlapping contributions are summed back.
+// Every tensor apply is the reference's three mxm passes (h1mg_tnsr3d_el,
+// hsmg.f:1320-1338) with left-to-right sums.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "nb_mg.h"
+
+namespace nb {
+
+Multigrid::~Multigrid() {
+  for (int l = 0; l < 8; ++l) {
+    MgLevel &L = lv[l];
+    gs_release(&L.gs);
+    gs_release(&L.gsx);
+    double *ps[] = {L.rstr_wt, L.fast_s, L.fast_d, L.schwarz_wt, L.jh, L.jht, L.e, L.r};
+    for (double *p : ps)
+      if (p) cudaFree(p);
+    if (L.mask) cudaFree(L.mask);
+  }
+  if (A) cudaFree(A);
+  if (B) cudaFree(B);
+  if (w) cudaFree(w);
+}
+
+namespace {
+
+// ---------------------------------------------------------------- device --
+// v(nv^3) = [Ct (x) Bt (x) A] u(nu^3): work = A u, work2 = work Bt per slab,
+// v = work2 Ct.  A is nv x nu, Bt and Ct are nu x nv, column-major.  All
+// operands in shared memory, the CTA cooperates; ends with a barrier.
+__device__ void tensor3(double *v, const double *u, int nv, int nu,
+                        const double *A, const double *Bt, const double *Ct,
+                        double *work, double *work2) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  const int nu2 = nu * nu;
+  for (int q = t; q < nv * nu2; q += nt) {  // work(a, n p) = sum_m A(a,m) u(m, n p)
+    const int a = q % nv, np_ = q / nv;
+    double s = mul_rn(A[a], u[np_ * nu]);
+    for (int m = 1; m < nu; ++m) s = fma_rn(A[a + m * nv], u[m + np_ * nu], s);
+    work[q] = s;
+  }
+  __syncthreads();
+  for (int q = t; q < nv * nv * nu; q += nt) {  // work2(a,b,p) = sum_n work(a,n,p) Bt(n,b)
+    const int a = q % nv, b = (q / nv) % nv, p = q / (nv * nv);
+    const double *wp = work + nv * nu * p;
+    double s = mul_rn(wp[a], Bt[b * nu]);
+    for (int n = 1; n < nu; ++n) s = fma_rn(wp[a + n * nv], Bt[n + b * nu], s);
+    work2[q] = s;
+  }
+  __syncthreads();
+  for (int q = t; q < nv * nv * nv; q += nt) {  // v(ab, c) = sum_p work2(ab,p) Ct(p,c)
+    const int ab = q % (nv * nv), c = q / (nv * nv);
+    double s = mul_rn(work2[ab], Ct[c * nu]);
+    for (int p = 1; p < nu; ++p) s = fma_rn(work2[ab + p * nv * nv], Ct[p + c * nu], s);
+    v[q] = s;
+  }
+  __syncthreads();
+}
+
+__device__ inline void load_shared(double *dst, const double *src, int n) {
+  for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
+}
+
+// ext index helpers: extended element has nl = nh+2 points per direction
+__device__ inline int ghost_face(int a, int b, int c, int nl) {
+  // returns 0 (not a ghost-face position), else 1 + axis*2 + (high side)
+  const int hi = nl - 1;
+  const bool ga = (a == 0 || a == hi), gb = (b == 0 || b == hi), gc = (c == 0 || c == hi);
+  if (ga && !gb && !gc) return 1 + (a == hi);
+  if (gb && !ga && !gc) return 3 + (b == hi);
+  if (gc && !ga && !gb) return 5 + (c == hi);
+  return 0;
+}
+
+// h1mg_schwarz_toext3d + extrude(A,0,0,A,2,1) (hsmg.f:1075-1077): regular
+// points copied into the extended array, each ghost face set to the
+// element's own layer-2 value, ghost edges and corners zero.
+__global__ void k_toext(double *A, const double *r, int nh, int nelt) {
+  const int nl = nh + 2;
+  const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh;
+  const long tot = nl3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / nl3;
+    const int rr = int(q % nl3);
+    int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
+    const int gf = ghost_face(a, b, c, nl);
+    double v = 0.0;
+    if (a >= 1 && a <= nh && b >= 1 && b <= nh && c >= 1 && c <= nh) {
+      v = r[e * nh3 + (a - 1) + nh * (b - 1) + long(nh) * nh * (c - 1)];
+    } else if (gf) {
+      if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
+      else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
+      else if (gf == 5) c = 2; else c = nl - 3;
+      v = r[e * nh3 + (a - 1) + nh * (b - 1) + long(nh) * nh * (c - 1)];
+    }
+    A[q] = v;
+  }
+}
+
+// extrude(A,0,1,A,2,-1) (hsmg.f:1079): ghost faces minus the own layer-2
+// value, leaving the neighbour's value
+__global__ void k_ghost_minus(double *A, int nh, int nelt) {
+  const int nl = nh + 2;
+  const long nl3 = long(nl) * nl * nl, tot = nl3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const int rr = int(q % nl3);
+    int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
+    const int gf = ghost_face(a, b, c, nl);
+    if (!gf) continue;
+    if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
+    else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
+    else if (gf == 5) c = 2; else c = nl - 3;
+    const long p = q - rr + a + long(nl) * b + long(nl) * nl * c;
+    A[q] = fma_rn(-1.0, A[p], A[q]);
+  }
+}
+
+// h1mg_do_fast (hsmg.f:1297-1318): B = S (d .* (S^T A)) per extended element;
+// also saves B's ghost faces into A (the first extrude of the overlap sum,
+// hsmg.f:1084: A <- 0*A + B on the ghost faces).
+__global__ void k_fdm(double *B, double *A, const double *s, const double *d,
+                      int nl) {
+  extern __shared__ double sm[];
+  const int nl2 = nl * nl, nl3 = nl2 * nl;
+  double *u = sm, *v = u + nl3, *work = v + nl3, *work2 = work + nl3,
+         *S = work2 + nl3;  // 6 matrices nl*nl
+  const long e = blockIdx.x;
+  load_shared(u, A + e * nl3, nl3);
+  load_shared(S, s + e * 6L * nl2, 6 * nl2);
+  __syncthreads();
+  // s(1,2,1)=S_r^T, s(1,1,2)=S_s, s(1,1,3)=S_t
+  tensor3(v, u, nl, nl, S + nl2, S + 2 * nl2, S + 4 * nl2, work, work2);
+  const double *de = d + e * nl3;
+  for (int q = threadIdx.x; q < nl3; q += blockDim.x) u[q] = mul_rn(de[q], v[q]);
+  __syncthreads();
+  // s(1,1,1)=S_r, s(1,2,2)=S_s^T, s(1,2,3)=S_t^T
+  tensor3(v, u, nl, nl, S, S + 3 * nl2, S + 5 * nl2, work, work2);
+  for (int q = threadIdx.x; q < nl3; q += blockDim.x) {
+    const int a = q % nl, b = (q / nl) % nl, c = q / nl2;
+    B[e * nl3 + q] = v[q];
+    if (ghost_face(a, b, c, nl)) A[e * nl3 + q] = v[q];
+  }
+}
+
+// extrude(B,0,1,A,0,-1), extrude(B,2,1,B,0,1), toreg3d (hsmg.f:1086-1090):
+// each regular point adds, in the reference's face order, the neighbour
+// contributions (gs'd ghost minus saved ghost) of the ghost faces whose
+// layer-2 partner it is.
+__global__ void k_overlap_toreg(double *e_out, const double *B, const double *A,
+                                int nh, int nelt) {
+  const int nl = nh + 2;
+  const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh, tot = nh3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / nh3;
+    const int rr = int(q % nh3);
+    const int a = rr % nh + 1, b = (rr / nh) % nh + 1, c = rr / (nh * nh) + 1;
+    const long base = e * nl3;
+    auto at = [&](int x, int y, int z) { return base + x + long(nl) * y + long(nl) * nl * z; };
+    double v = B[at(a, b, c)];
+    if (a == 2) { const long g = at(0, b, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    if (a == nl - 3) { const long g = at(nl - 1, b, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    if (b == 2) { const long g = at(a, 0, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    if (b == nl - 3) { const long g = at(a, nl - 1, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    if (c == 2) { const long g = at(a, b, 0); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    if (c == nl - 3) { const long g = at(a, b, nl - 1); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    e_out[q] = v;
+  }
+}
+
+// h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps
+__global__ void k_schwarz_wt(double *e, const double *wt, int n, int nelt) {
+  const long n3 = long(n) * n * n, tot = n3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const long el = q / n3;
+    const int rr = int(q % n3);
+    const int i = rr % n, j = (rr / n) % n, k = rr / (n * n);
+    const double *we = wt + el * 12L * n * n;
+    auto W = [&](int a, int b, int s, int d) {
+      return we[a + n * b + n * n * s + 4 * n * n * d];
+    };
+    const int L[4] = {0, 1, n - 2, n - 1};
+    double v = e[q];
+    bool done = false;
+    for (int s = 0; s < 4; ++s)
+      if (i == L[s]) { v = mul_rn(v, sqrt(W(j, k, s, 0))); done = true; }
+    if (!done && i >= 2 && i <= n - 3) {
+      for (int s = 0; s < 4; ++s)
+        if (j == L[s]) { v = mul_rn(v, sqrt(W(i, k, s, 1))); done = true; }
+      if (!done && j >= 2 && j <= n - 3)
+        for (int s = 0; s < 4; ++s)
+          if (k == L[s]) v = mul_rn(v, sqrt(W(i, j, s, 2)));
+    }
+    e[q] = v;
+  }
+}
+
+// h1mg_rstr (hsmg.f:1340-1360): do_wt (hsmg.f:1362-1391) then
+// v = [J^T (x) J^T (x) J^T] u per element
+__global__ void k_rstr(double *v, const double *u, const double *wt, int nu,
+                       int nv, const double *jht, const double *jh) {
+  extern __shared__ double sm[];
+  const int nu3 = nu * nu * nu, nmax = max(nu, nv), nmax3 = nmax * nmax * nmax;
+  double *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3,
+         *Jt = work2 + nmax3, *J = Jt + nu * nv;
+  const long e = blockIdx.x;
+  const double *we = wt + e * 6L * nu * nu;
+  for (int q = threadIdx.x; q < nu3; q += blockDim.x) {
+    const int i = q % nu, j = (q / nu) % nu, k = q / (nu * nu);
+    double x = u[e * nu3 + q];
+    if (i == 0) x = mul_rn(x, we[j + nu * k + 0]);
+    else if (i == nu - 1) x = mul_rn(x, we[j + nu * k + nu * nu]);
+    else if (j == 0) x = mul_rn(x, we[i + nu * k + 2 * nu * nu]);
+    else if (j == nu - 1) x = mul_rn(x, we[i + nu * k + 3 * nu * nu]);
+    else if (k == 0) x = mul_rn(x, we[i + nu * j + 4 * nu * nu]);
+    else if (k == nu - 1) x = mul_rn(x, we[i + nu * j + 5 * nu * nu]);
+    us[q] = x;
+  }
+  load_shared(Jt, jht, nu * nv);
+  load_shared(J, jh, nu * nv);
+  __syncthreads();
+  tensor3(vs, us, nv, nu, Jt, J, J, work, work2);
+  const int nv3 = nv * nv * nv;
+  for (int q = threadIdx.x; q < nv3; q += blockDim.x) v[e * nv3 + q] = vs[q];
+}
+
+// h1mg_intp (hsmg.f:1436-1475) accumulated: out += [J (x) J (x) J] uc
+__global__ void k_intp_add(double *out, const double *uc, int nu, int nv,
+                           const double *jh, const double *jht) {
+  extern __shared__ double sm[];
+  const int nmax = max(nu, nv), nmax3 = nmax * nmax * nmax;
+  double *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3,
+         *J = work2 + nmax3, *Jt = J + nu * nv;
+  const long e = blockIdx.x;
+  const int nu3 = nu * nu * nu, nv3 = nv * nv * nv;
+  load_shared(us, uc + e * nu3, nu3);
+  load_shared(J, jh, nu * nv);
+  load_shared(Jt, jht, nu * nv);
+  __syncthreads();
+  tensor3(vs, us, nv, nu, J, Jt, Jt, work, work2);
+  for (int q = threadIdx.x; q < nv3; q += blockDim.x)
+    out[e * nv3 + q] = add_rn(out[e * nv3 + q], vs[q]);
+}
+
+// set-up helpers -------------------------------------------------------
+__global__ void k_fill(double *a, double v, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = v;
+}
+// element faces = 1, rest 0 (h1mg_setup_rstr_wt, hsmg.f:211-229)
+__global__ void k_faces_one(double *w, int n, int nelt) {
+  const long n3 = long(n) * n * n, tot = n3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const int rr = int(q % n3);
+    const int i = rr % n, j = (rr / n) % n, k = rr / (n * n);
+    w[q] = (i == 0 || i == n - 1 || j == 0 || j == n - 1 || k == 0 || k == n - 1) ? 1.0 : 0.0;
+  }
+}
+// wt(.,.,side,dir,e) = 1/w at the element faces (hsmg.f:233-247)
+__global__ void k_rstr_wt(double *wt, const double *w, int n, int nelt) {
+  const long n2 = long(n) * n, tot = n2 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / n2;
+    const int a = int(q % n2) % n, b = int(q % n2) / n;
+    const double *we = w + e * n2 * n;
+    double *te = wt + e * 6 * n2;
+    te[a + n * b + 0 * n2] = 1.0 / we[0 + n * a + n2 * b];
+    te[a + n * b + 1 * n2] = 1.0 / we[(n - 1) + n * a + n2 * b];
+    te[a + n * b + 2 * n2] = 1.0 / we[a + n * 0 + n2 * b];
+    te[a + n * b + 3 * n2] = 1.0 / we[a + n * (n - 1) + n2 * b];
+    te[a + n * b + 4 * n2] = 1.0 / we[a + n * b + n2 * 0];
+    te[a + n * b + 5 * n2] = 1.0 / we[a + n * b + n2 * (n - 1)];
+  }
+}
+// save ghost faces of B into A (setup version of the k_fdm side effect)
+__global__ void k_save_ghost(double *A, const double *B, int nl, int nelt) {
+  const long nl3 = long(nl) * nl * nl, tot = nl3 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const int rr = int(q % nl3);
+    if (ghost_face(rr % nl, (rr / nl) % nl, rr / (nl * nl), nl)) A[q] = B[q];
+  }
+}
+// schwarz wt = 1/work at layers 1,2,n-1,n (h1mg_setup_schwarz_wt3d_2,
+// hsmg.f:653-688)
+__global__ void k_schwarz_wt_setup(double *wt, const double *w, int n, int nelt) {
+  const long n2 = long(n) * n, tot = n2 * nelt;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / n2;
+    const int a = int(q % n2) % n, b = int(q % n2) / n;
+    const double *we = w + e * n2 * n;
+    double *te = wt + e * 12 * n2;
+    const int L[4] = {0, 1, n - 2, n - 1};
+    for (int s = 0; s < 4; ++s) {
+      te[a + n * b + n2 * s + 0 * 4 * n2] = 1.0 / we[L[s] + n * a + n2 * b];
+      te[a + n * b + n2 * s + 1 * 4 * n2] = 1.0 / we[a + n * L[s] + n2 * b];
+      te[a + n * b + n2 * s + 2 * 4 * n2] = 1.0 / we[a + n * b + n2 * L[s]];
+    }
+  }
+}
+
+int grid_for(long n) { return int(std::max(1L, std::min<long>(152L * 8, (n + 255) / 256))); }
+
+size_t tensor_smem(int nmax, int extra) {
+  return sizeof(double) * (4 * size_t(nmax) * nmax * nmax + extra);
+}
+
+int set_smem(const void *fn, size_t bytes) {
+  NB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+  return NB_OK;
+}
+
+template <typename T>
+int dmalloc(T **p, size_t n) {
+  NB_CUDA(cudaMalloc(p, sizeof(T) * std::max<size_t>(n, 1)));
+  return NB_OK;
+}
+template <typename T>
+int upload(T **p, const std::vector<T> &h) {
+  NB_TRY(dmalloc(p, h.size()));
+  if (!h.empty())
+    NB_CUDA(cudaMemcpy(*p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  return NB_OK;
+}
+
+// host gather-scatter sum (jl semantics) for set-up quantities
+void gs_host_add(const GsHost &g, double *u) {
+  const uint32_t END = uint32_t(-1);
+  auto gather = [&](const std::vector<uint32_t> &m) {
+    size_t p = 0;
+    while (m[p] != END) {
+      const uint32_t i = m[p++];
+      double t = u[i];
+      while (m[p] != END) t += u[m[p++]];
+      ++p;
+      u[i] = t;
+    }
+  };
+  auto scatter = [&](const std::vector<uint32_t> &m) {
+    size_t p = 0;
+    while (m[p] != END) {
+      const uint32_t i = m[p++];
+      while (m[p] != END) u[m[p++]] = u[i];
+      ++p;
+    }
+  };
+  gather(g.map[0]);
+  for (size_t q = 0; q + 1 < g.map[2].size(); ++q) u[g.map[2][q]] = 0.0;
+  scatter(g.map[1]);
+}
+
+// h1mg_setup_fast1d_a / _b (hsmg.f:403-481); a, b are (n+3)^2 column-major
+void fast1d_ab(double *a, double *b, int lbc, int rbc, double ll, double lm,
+               double lr, const double *ah, const double *bh, int n) {
+  const int na = n + 3;
+  auto A = [&](int i, int j) -> double & { return a[i + j * na]; };
+  auto Bm = [&](int i, int j) -> double & { return b[i + j * na]; };
+  auto AH = [&](int i, int j) { return ah[i + j * (n + 1)]; };
+  const int i0 = lbc == 1 ? 1 : 0, i1 = rbc == 1 ? n - 1 : n;
+  for (int q = 0; q < na * na; ++q) a[q] = b[q] = 0.;
+  double fac = 2.0 / lm;
+  A(1, 1) = 1.0;
+  A(n + 1, n + 1) = 1.0;
+  for (int j = i0; j <= i1; ++j)
+    for (int i = i0; i <= i1; ++i) A(i + 1, j + 1) = fac * AH(i, j);
+  if (lbc == 0) {
+    fac = 2.0 / ll;
+    A(0, 0) = fac * AH(n - 1, n - 1);
+    A(1, 0) = fac * AH(n, n - 1);
+    A(0, 1) = fac * AH(n - 1, n);
+    A(1, 1) = A(1, 1) + fac * AH(n, n);
+  } else {
+    A(0, 0) = 1.0;
+  }
+  if (rbc == 0) {
+    fac = 2.0 / lr;
+    A(n + 1, n + 1) = A(n + 1, n + 1) + fac * AH(0, 0);
+    A(n + 2, n + 1) = fac * AH(1, 0);
+    A(n + 1, n + 2) = fac * AH(0, 1);
+    A(n + 2, n + 2) = fac * AH(1, 1);
+  } else {
+    A(n + 2, n + 2) = 1.0;
+  }
+  fac = 0.5 * lm;
+  Bm(1, 1) = 1.0;
+  Bm(n + 1, n + 1) = 1.0;
+  for (int i = i0; i <= i1; ++i) Bm(i + 1, i + 1) = fac * bh[i];
+  if (lbc == 0) {
+    fac = 0.5 * ll;
+    Bm(0, 0) = fac * bh[n - 1];
+    Bm(1, 1) = Bm(1, 1) + fac * bh[n];
+  } else {
+    Bm(0, 0) = 1.0;
+  }
+  if (rbc == 0) {
+    fac = 0.5 * lr;
+    Bm(n + 1, n + 1) = Bm(n + 1, n + 1) + fac * bh[0];
+    Bm(n + 2, n + 2) = fac * bh[1];
+  } else {
+    Bm(n + 2, n + 2) = 1.0;
+  }
+}
+
+// h1mg_setup_fast1d (hsmg.f:380-401): s(nl,nl,2) and eigenvalues
+int fast1d(double *s, double *lam, int nl, int lbc, int rbc, double ll,
+           double lm, double lr, const double *ah, const double *bh, int n) {
+  std::vector<double> b(nl * nl);
+  fast1d_ab(s, b.data(), lbc, rbc, ll, lm, lr, ah, bh, n);
+  const int info = generalev(s, b.data(), lam, nl);
+  if (info) return fail(NB_ERR_NUMERIC, "h1mg setup: generalized eigensolve failed (%d)", info);
+  auto rowz = [&](int e) {
+    for (int j = 0; j < nl; ++j) s[(e - 1) + j * nl] = 0.;
+  };
+  if (lbc > 0) rowz(1);
+  if (lbc == 1) rowz(2);
+  if (rbc > 0) rowz(nl);
+  if (rbc == 1) rowz(nl - 1);
+  for (int j = 0; j < nl; ++j)
+    for (int i = 0; i < nl; ++i) s[nl * nl + i + j * nl] = s[j + i * nl];
+  return NB_OK;
+}
+
+std::vector<int> level_mask(const Operator &op, int nh) {
+  std::vector<int> list;
+  const long n3 = long(nh) * nh * nh;
+  for (int e = 0; e < op.nelt; ++e) {
+    const unsigned f = op.face[e];
+    if (!f) continue;
+    for (int k = 0; k < nh; ++k)
+      for (int j = 0; j < nh; ++j)
+        for (int i = 0; i < nh; ++i) {
+          const bool m = ((f & 1u) && i == 0) || ((f & 2u) && i == nh - 1) ||
+                         ((f & 4u) && j == 0) || ((f & 8u) && j == nh - 1) ||
+                         ((f & 16u) && k == 0) || ((f & 32u) && k == nh - 1);
+          if (m) list.push_back(int(n3 * e + i + nh * j + nh * nh * k));
+        }
+  }
+  return list;
+}
+
+GsHost numbering(const Operator &op, int nx) {
+  const long n = long(nx) * nx * nx * op.nelt;
+  std::vector<int64_t> glo(n);
+  set_vert_box(glo.data(), nx, op.nelt, op.nelx, op.nely, op.lglel.data());
+  GsHost h;
+  gs_topology(glo.data(), int(n), &h);
+  return h;
+}
+
+// the sum-overlap sequence of h1mg_schwarz_part1 (hsmg.f:1083-1090) from B
+// (extended) into e (regular), with A as the ghost save area
+int overlap_sum(const MgLevel &L, int nelt, double *e, double *B, double *A,
+                cudaStream_t s) {
+  k_save_ghost<<<grid_for(L.next), 256, 0, s>>>(A, B, L.nl, nelt);
+  NB_TRY(gs_exec(L.gsx, B, 1, 1, 0, s));
+  k_overlap_toreg<<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+}  // namespace
+
+int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
+             cudaStream_t s) {
+  mg->op = &op;
+  const int nx1 = op.lx, nelt = op.nelt;
+  int ord[8] = {0};
+  if (!orders) {
+    static const int mgn2[10] = {1, 2, 2, 2, 2, 3, 3, 5, 5, 5};
+    if (nx1 > 10)
+      return fail(NB_ERR_UNSUPPORTED,
+                  "h1mg_setup: the reference level choice reads an undefined "
+                  "variable for lx1 > 10 (hsmg.f:65); pass explicit orders");
+    if (nx1 < 4) return fail(NB_ERR_UNSUPPORTED, "h1mg_setup: lx1=%d < 4", nx1);
+    int lmax = nx1 == 4 ? 2 : 3;
+    int m2 = mgn2[nx1 - 1];
+    if (nx1 == 8) m2 = 3;
+    m2 = std::min(3, m2);
+    ord[1] = 1;
+    ord[2] = m2;
+    ord[3] = m2 + 1;
+    ord[lmax] = nx1 - 1;
+    nlev = lmax;
+  } else {
+    if (nlev < 2 || nlev > 7) return fail(NB_ERR_ARG, "h1mg_setup: nlev=%d", nlev);
+    for (int l = 1; l <= nlev; ++l) ord[l] = orders[l - 1];
+    if (ord[nlev] != nx1 - 1)
+      return fail(NB_ERR_ARG, "h1mg_setup: finest order %d != lx1-1", ord[nlev]);
+  }
+  for (int l = 1; l <= nlev; ++l)
+    if (ord[l] < 1 || ord[l] + 3 > kMaxNl)
+      return fail(NB_ERR_UNSUPPORTED, "h1mg_setup: level order %d", ord[l]);
+  mg->nlev = nlev;
+  std::vector<std::vector<double>> ah(nlev + 1), bh(nlev + 1), zh(nlev + 1);
+  int maxnl = 0;
+  for (int l = 1; l <= nlev; ++l) {
+    MgLevel &L = mg->lv[l];
+    L.order = ord[l];
+    L.nh = ord[l] + 1;
+    L.nl = L.nh + 2;
+    L.n = long(L.nh) * L.nh * L.nh * nelt;
+    L.next = long(L.nl) * L.nl * L.nl * nelt;
+    maxnl = std::max(maxnl, L.nl);
+    const int nh = L.nh;
+    ah[l].resize(nh * nh);
+    bh[l].resize(nh);
+    zh[l].resize(nh);
+    std::vector<double> c(nh * nh), d(nh * nh);
+    semhat(ah[l].data(), bh[l].data(), c.data(), d.data(), zh[l].data(), ord[l]);
+    L.gs_host = numbering(op, nh);
+    L.gsx_host = numbering(op, nh + 2);
+    NB_TRY(gs_upload(L.gs_host, int(L.n), &L.gs, s));
+    NB_TRY(gs_upload(L.gsx_host, int(L.next), &L.gsx, s));
+    NB_TRY(dmalloc(&L.e, L.n));
+    NB_TRY(dmalloc(&L.r, L.n));
+    const std::vector<int> mk = level_mask(op, nh);
+    L.nmask = int(mk.size());
+    NB_TRY(upload(&L.mask, mk));
+  }
+  // interpolation (h1mg_setup_intp / _intpm, hsmg.f:120-152)
+  for (int l = 1; l < nlev; ++l) {
+    const int nf = mg->lv[l + 1].nh, nc = mg->lv[l].nh;
+    std::vector<double> jh(nf * nc), jht(nf * nc), w(2 * nc + 2);
+    for (int i = 0; i < nf; ++i) {
+      fd_weights_full(zh[l + 1][i], zh[l].data(), nc - 1, 1, w.data());
+      for (int j = 0; j < nc; ++j) jh[i + j * nf] = w[j];
+    }
+    for (int j = 0; j < nc; ++j)
+      for (int i = 0; i < nf; ++i) jht[j + i * nc] = jh[i + j * nf];
+    NB_TRY(upload(&mg->lv[l].jh, jh));
+    NB_TRY(upload(&mg->lv[l].jht, jht));
+  }
+  const long maxext = long(maxnl) * maxnl * maxnl * nelt;
+  NB_TRY(dmalloc(&mg->A, maxext));
+  NB_TRY(dmalloc(&mg->B, maxext));
+  NB_TRY(dmalloc(&mg->w, op.n));
+  // restriction weights
+  for (int l = 1; l <= nlev; ++l) {
+    MgLevel &L = mg->lv[l];
+    NB_TRY(dmalloc(&L.rstr_wt, size_t(L.nh) * L.nh * 6 * nelt));
+    k_faces_one<<<grid_for(L.n), 256, 0, s>>>(mg->A, L.nh, nelt);
+    NB_TRY(gs_exec(L.gs, mg->A, 1, 1, 0, s));
+    k_rstr_wt<<<grid_for(long(L.nh) * L.nh * nelt), 256, 0, s>>>(L.rstr_wt, mg->A, L.nh, nelt);
+    NB_CUDA(cudaGetLastError());
+  }
+  // FDM (h1mg_setup_fdm / _fast, hsmg.f:251-378): element lengths through a
+  // dssum of face-centre markers on the finest numbering
+  {
+    const int lx = nx1;
+    const long nxyz = long(lx) * lx * lx;
+    std::vector<double> lw(op.n, 0.0);
+    const double lm = 2.0;
+    auto at = [&](int i, int j, int k, int e) -> double & {
+      return lw[(i - 1) + lx * (j - 1) + long(lx) * lx * (k - 1) + nxyz * e];
+    };
+    for (int e = 0; e < nelt; ++e) {
+      at(1, 2, 2, e) = lm;
+      at(lx, 2, 2, e) = lm;
+      at(2, 1, 2, e) = lm;
+      at(2, lx, 2, e) = lm;
+      at(2, 2, 1, e) = lm;
+      at(2, 2, lx, e) = lm;
+    }
+    gs_host_add(op.gsh_host, lw.data());
+    for (int l = 2; l <= nlev; ++l) {
+      MgLevel &L = mg->lv[l];
+      const int nl = L.nl, n = L.order;
+      std::vector<double> S(size_t(nl) * nl * 6 * nelt), Dd(size_t(nl) * nl * nl * nelt);
+      std::vector<double> lr(nl), ls(nl), lt(nl);
+      for (int e = 0; e < nelt; ++e) {
+        const double llr = at(1, 2, 2, e) - lm, lrr = at(lx, 2, 2, e) - lm;
+        const double lls = at(2, 1, 2, e) - lm, lrs = at(2, lx, 2, e) - lm;
+        const double llt = at(2, 2, 1, e) - lm, lrt = at(2, 2, lx, e) - lm;
+        const unsigned f = op.face[e];
+        double *se = S.data() + size_t(nl) * nl * 6 * e;
+        NB_TRY(fast1d(se, lr.data(), nl, f & 1u ? 1 : 0, f & 2u ? 1 : 0, llr, lm, lrr,
+                      ah[l].data(), bh[l].data(), n));
+        NB_TRY(fast1d(se + 2 * nl * nl, ls.data(), nl, f & 4u ? 1 : 0, f & 8u ? 1 : 0, lls,
+                      lm, lrs, ah[l].data(), bh[l].data(), n));
+        NB_TRY(fast1d(se + 4 * nl * nl, lt.data(), nl, f & 16u ? 1 : 0, f & 32u ? 1 : 0, llt,
+                      lm, lrt, ah[l].data(), bh[l].data(), n));
+        auto vmax = [&](const std::vector<double> &v) {
+          double t = -99.0e20;
+          for (int q = 1; q <= nl - 2; ++q) t = std::max(t, v[q]);
+          return t;
+        };
+        const double eps = 1.e-5 * (vmax(lr) + vmax(ls) + vmax(lt));
+        double *de = Dd.data() + size_t(nl) * nl * nl * e;
+        int il = 0;
+        for (int k = 0; k < nl; ++k)
+          for (int j = 0; j < nl; ++j)
+            for (int i = 0; i < nl; ++i) {
+              const double diag = lr[i] + ls[j] + lt[k];
+              de[il++] = diag > eps ? 1.0 / diag : 0.0;
+            }
+      }
+      NB_TRY(upload(&L.fast_s, S));
+      NB_TRY(upload(&L.fast_d, Dd));
+    }
+  }
+  // Schwarz weights (h1mg_setup_schwarz_wt3d_1, hsmg.f:572-622)
+  for (int l = 2; l <= nlev; ++l) {
+    MgLevel &L = mg->lv[l];
+    NB_TRY(dmalloc(&L.schwarz_wt, size_t(L.nh) * L.nh * 12 * nelt));
+    k_fill<<<grid_for(L.next), 256, 0, s>>>(mg->B, 1.0, L.next);
+    NB_TRY(overlap_sum(L, nelt, L.e, mg->B, mg->A, s));
+    NB_TRY(gs_exec(L.gs, L.e, 1, 1, 0, s));
+    k_schwarz_wt_setup<<<grid_for(long(L.nh) * L.nh * nelt), 256, 0, s>>>(L.schwarz_wt, L.e,
+                                                                        L.nh, nelt);
+    NB_CUDA(cudaGetLastError());
+  }
+  const size_t sm_fdm = sizeof(double) * (4 * size_t(maxnl) * maxnl * maxnl + 6 * maxnl * maxnl);
+  if (sm_fdm > 227 * 1024)
+    return fail(NB_ERR_UNSUPPORTED, "h1mg: extended element of %d points too large", maxnl);
+  NB_TRY(set_smem((const void *)k_fdm, sm_fdm));
+  NB_TRY(set_smem((const void *)k_rstr, tensor_smem(maxnl, 2 * maxnl * maxnl)));
+  NB_TRY(set_smem((const void *)k_intp_add, tensor_smem(maxnl, 2 * maxnl * maxnl)));
+  NB_CUDA(cudaStreamSynchronize(s));
+  return NB_OK;
+}
+
+namespace {
+
+// h1mg_schwarz (hsmg.f:1036-1051) at level l: e = sqrt(W) part1(r); masks r
+int mg_schwarz(Multigrid &mg, double *e, double *r, int l, cudaStream_t s) {
+  MgLevel &L = mg.lv[l];
+  const int nelt = mg.op->nelt;
+  NB_TRY(vec_mask<double>(r, L.mask, L.nmask, s));
+  k_toext<<<grid_for(L.next), 256, 0, s>>>(mg.A, r, L.nh, nelt);
+  NB_TRY(gs_exec(L.gsx, mg.A, 1, 1, 0, s));
+  k_ghost_minus<<<grid_for(L.next), 256, 0, s>>>(mg.A, L.nh, nelt);
+  const int nl = L.nl;
+  const size_t sm = sizeof(double) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
+  k_fdm<<<nelt, 256, sm, s>>>(mg.B, mg.A, L.fast_s, L.fast_d, nl);
+  NB_CUDA(cudaGetLastError());
+  NB_TRY(gs_exec(L.gsx, mg.B, 1, 1, 0, s));
+  k_overlap_toreg<<<grid_for(L.n), 256, 0, s>>>(e, mg.B, mg.A, L.nh, nelt);
+  NB_TRY(gs_exec(L.gs, e, 1, 1, 0, s));
+  NB_TRY(vec_mask<double>(e, L.mask, L.nmask, s));
+  k_schwarz_wt<<<grid_for(L.n), 256, 0, s>>>(e, L.schwarz_wt, L.nh, nelt);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+int mg_rstr(Multigrid &mg, double *rc, const double *rf, int l, bool dssum,
+            cudaStream_t s) {
+  const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
+  const int nmax = std::max(F.nh, C.nh);
+  k_rstr<<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh), s>>>(
+      rc, rf, F.rstr_wt, F.nh, C.nh, C.jht, C.jh);
+  NB_CUDA(cudaGetLastError());
+  if (dssum) NB_TRY(gs_exec(C.gs, rc, 1, 1, 0, s));
+  return NB_OK;
+}
+
+int mg_intp_add(Multigrid &mg, double *of, const double *ec, int l, cudaStream_t s) {
+  const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
+  const int nmax = std::max(F.nh, C.nh);
+  k_intp_add<<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh), s>>>(
+      of, ec, C.nh, F.nh, C.jh, C.jht);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+}  // namespace
+
+int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s) {
+  const int Lm = mg.nlev;
+  MgLevel &T = mg.lv[Lm];
+  NB_TRY(mg_schwarz(mg, z, rhs, Lm, s));
+  NB_TRY(vec_copy<double>(T.r, rhs, T.n, s));
+  for (int l = Lm - 1; l >= 2; --l) {
+    NB_TRY(mg_rstr(mg, mg.lv[l].r, mg.lv[l + 1].r, l, true, s));
+    NB_TRY(mg_schwarz(mg, mg.lv[l].e, mg.lv[l].r, l, s));
+  }
+  MgLevel &C = mg.lv[1];
+  NB_TRY(mg_rstr(mg, C.r, mg.lv[2].r, 1, false, s));
+  NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
+  NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));  // hsmg_coarse_solve
+  NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
+  NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
+  for (int l = 2; l <= Lm - 1; ++l) NB_TRY(mg_intp_add(mg, mg.lv[l].e, mg.lv[l - 1].e, l - 1, s));
+  return mg_intp_add(mg, z, mg.lv[Lm - 1].e, Lm - 1, s);
+}
+
+}  // namespace nb

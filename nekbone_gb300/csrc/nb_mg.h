@@ -1,0 +1,42 @@
+// nb_mg.h -- hybrid Schwarz multigrid (hsmg.f) on the GPU.
+#pragma once
+
+#include <vector>
+
+#include "nb_solver.h"
+
+namespace nb {
+
+struct MgLevel {
+  int order = 0, nh = 0, nl = 0;  // polynomial order, points, extended points
+  long n = 0, next = 0;           // nh^3*nelt, nl^3*nelt
+  GsHost gs_host, gsx_host;       // regular and Schwarz (extended) numbering
+  GsDevice gs, gsx;
+  double *rstr_wt = nullptr;      // (nh,nh,2,3,nelt)   hsmg.f:201-249
+  double *fast_s = nullptr;       // (nl*nl,2,3,nelt)   hsmg.f:285-378
+  double *fast_d = nullptr;       // (nl^3,nelt)
+  double *schwarz_wt = nullptr;   // (nh,nh,4,3,nelt)   hsmg.f:572-688
+  int *mask = nullptr;            // masked points at this level
+  int nmask = 0;
+  double *jh = nullptr, *jht = nullptr;  // to the next finer level (nf x nc)
+  double *e = nullptr, *r = nullptr;     // level vectors
+};
+
+struct Multigrid {
+  const Operator *op = nullptr;
+  int nlev = 0;
+  MgLevel lv[8];                  // 1-based
+  double *A = nullptr, *B = nullptr;  // extended work arrays (finest size)
+  double *w = nullptr;            // interpolation result
+  ~Multigrid();
+};
+
+// h1mg_setup (hsmg.f:3-29).  orders == nullptr: the reference's level
+// choice (h1mg_setup_mg_nx, hsmg.f:45-97; defined only for lx1 <= 10);
+// otherwise nlev polynomial orders, coarsest first, the last = lx1-1.
+int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
+             cudaStream_t s);
+// h1mg_solve (hsmg.f:960-1034): z = M^-1 rhs; masks rhs in place.
+int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s);
+
+}  // namespace nb

@@ -1,0 +1,260 @@
+// nb_mixed.cu -- device set-up helpers, FP64 CG to a tolerance, and the
+// mixed-precision solver: FP32 inner CG (ax, gather-scatter and vector
+// updates in FP32) inside an FP64 defect-correction loop.  The reference has
+// no counterpart for these solvers (its cg runs a fixed niter, cg.f:48-75);
+// they reuse the same operator, numbering, mask and norm
+// sqrt(r'Cr) (cg.f:42,66-69).
+#include <cmath>
+#include <memory>
+#include <vector>
+
+#include "../../include/nekbone_gb300.h"
+#include "nb_solver.h"
+
+namespace nb {
+
+namespace {
+
+int grid_for(long n) {
+  return int(std::max(1L, std::min<long>(152L * 8, (n + 255) / 256)));
+}
+
+// setup_g (prox_setup.f:27-52) from the GLL weights
+__global__ void k_setup_g(double *g, const double *wgt, int lx, long n) {
+  const long l3 = long(lx) * lx * lx;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    const int r = int(q % l3);
+    const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+    const double v = wgt[i] * wgt[j] * wgt[k];
+    double *gp = g + 6 * q;
+    gp[0] = v;
+    gp[1] = 0.;
+    gp[2] = 0.;
+    gp[3] = v;
+    gp[4] = 0.;
+    gp[5] = v;
+  }
+}
+
+// counter-based uniform [-1,1) keyed by (seed, global id): splitmix64 finaliser
+__device__ __forceinline__ double uniform_pm1(uint64_t seed, uint64_t id) {
+  uint64_t z = seed * 0x9E3779B97F4A7C15ull + id + 0x632BE59BD9B4E019ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return double(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+// box global id of local point q (set_vert_box, prox_dssum.f:42-73) for the
+// brick order lglel(e) = e
+__global__ void k_rhs_uniform(double *f, int lx, int nelx, int nely, long n,
+                              uint64_t seed) {
+  const long l3 = long(lx) * lx * lx;
+  const int nn = lx - 1;
+  const long ax = long(nn) * nelx + 1, ay = long(nn) * nely + 1;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / l3;
+    const int r = int(q % l3);
+    const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+    const long ex = e % nelx, ey = (e / nelx) % nely, ez = e / (long(nelx) * nely);
+    const long id = 1 + (nn * ex + i) + (nn * ey + j) * ax + (nn * ez + k) * ax * ay;
+    f[q] = uniform_pm1(seed, uint64_t(id));
+  }
+}
+
+__global__ void k_col2(double *a, const double *b, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = mul_rn(a[q], b[q]);
+}
+
+// r = f - w
+__global__ void k_residual(double *r, const double *f, const double *w, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    r[q] = f[q] - w[q];
+}
+
+// x += scale * double(e)
+__global__ void k_axpy_f32(double *x, const float *e, double scale, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    x[q] = fma_rn(scale, double(e[q]), x[q]);
+}
+
+// y = float(scale * r)
+__global__ void k_scale_f32(float *y, const double *r, double scale, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    y[q] = float(r[q] * scale);
+}
+
+}  // namespace
+
+int dev_setup_g(const Operator &op, double *g, cudaStream_t s) {
+  const int lx = op.lx;
+  std::vector<double> a(lx * lx), b(lx), c(lx * lx), d(lx * lx), z(lx);
+  semhat(a.data(), b.data(), c.data(), d.data(), z.data(), lx - 1);
+  double *dw = nullptr;
+  NB_CUDA(cudaMalloc(&dw, lx * sizeof(double)));
+  NB_CUDA(cudaMemcpy(dw, b.data(), lx * sizeof(double), cudaMemcpyHostToDevice));
+  k_setup_g<<<grid_for(op.n), 256, 0, s>>>(g, dw, lx, op.n);
+  NB_CUDA(cudaGetLastError());
+  NB_CUDA(cudaStreamSynchronize(s));
+  cudaFree(dw);
+  return NB_OK;
+}
+
+// f = uniform[-1,1) per global point, dssum, times c, masked (the set_f
+// sequence of driver.f:88-101 with a seeded, layout-independent source)
+int dev_rhs_uniform(const Operator &op, double *f, const double *c,
+                    uint64_t seed, cudaStream_t s) {
+  k_rhs_uniform<<<grid_for(op.n), 256, 0, s>>>(f, op.lx, op.nelx, op.nely, op.n, seed);
+  NB_CUDA(cudaGetLastError());
+  NB_TRY(gs_exec(op.gs, f, 1, 1, 0, s));
+  k_col2<<<grid_for(op.n), 256, 0, s>>>(f, c, op.n);
+  NB_CUDA(cudaGetLastError());
+  NB_TRY(vec_mask<double>(f, op.d_mask_list, op.n_mask, s));
+  return NB_OK;
+}
+
+int dev_residual(const Operator &op, double *r, const double *f,
+                 const double *w, long n, cudaStream_t s) {
+  (void)op;
+  k_residual<<<grid_for(n), 256, 0, s>>>(r, f, w, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+int dev_axpy_f32(double *x, const float *e, double scale, long n, cudaStream_t s) {
+  k_axpy_f32<<<grid_for(n), 256, 0, s>>>(x, e, scale, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+int dev_scale_to_f32(float *y, const double *r, double scale, long n, cudaStream_t s) {
+  k_scale_f32<<<grid_for(n), 256, 0, s>>>(y, r, scale, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+cudaStream_t lib_stream();
+
+}  // namespace nb
+
+using namespace nb;
+
+extern "C" {
+
+// Declared here, defined in nb_abi.cpp: access to a mesh's operator/workspace.
+int nb_mesh_parts(nb_mesh *mesh, void **op, void **wk);
+
+int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
+              const double *c, double tol, int max_iter, int check_every,
+              int *iters, double *relres) {
+  clear_status();
+  void *pop = nullptr, *pwk = nullptr;
+  NB_TRY(nb_mesh_parts(mesh, &pop, &pwk));
+  Operator &op = *static_cast<Operator *>(pop);
+  CgWork &wk = *static_cast<CgWork *>(pwk);
+  cudaStream_t s = lib_stream();
+  const long n = op.n;
+  if (check_every < 1) check_every = 1;
+  double *r, *w, *p;
+  NB_CUDA(cudaMalloc(&r, n * 8));
+  NB_CUDA(cudaMalloc(&w, n * 8));
+  NB_CUDA(cudaMalloc(&p, n * 8));
+  int done = 0;
+  double rn0 = 0, rn = 0;
+  // run CG in chunks: cg_device always starts from x=0, so iterate one long
+  // solve with the device scalars and poll rnorm every check_every steps.
+  int st = cg_begin(op, wk, x, f, c, r, max_iter, s);
+  if (!st) {
+    NB_CUDA(cudaMemcpyAsync(&rn0, &wk.sc->rnorm, 8, cudaMemcpyDeviceToHost, s));
+    NB_CUDA(cudaStreamSynchronize(s));
+    rn = rn0;
+    while (done < max_iter && !st) {
+      const int k = std::min(check_every, max_iter - done);
+      st = cg_steps(op, wk, x, g, c, r, w, p, done + 1, done + k, s);
+      done += k;
+      NB_CUDA(cudaMemcpyAsync(&rn, &wk.sc->rnorm, 8, cudaMemcpyDeviceToHost, s));
+      NB_CUDA(cudaStreamSynchronize(s));
+      if (rn0 > 0 && rn / rn0 <= tol) break;
+    }
+  }
+  cudaFree(r);
+  cudaFree(w);
+  cudaFree(p);
+  if (st) return st;
+  if (iters) *iters = done;
+  if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
+  return NB_OK;
+}
+
+int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
+                const double *c, double tol, int inner_iters, int max_outer,
+                int *outer, int *inner_total, double *relres) {
+  clear_status();
+  void *pop = nullptr, *pwk = nullptr;
+  NB_TRY(nb_mesh_parts(mesh, &pop, &pwk));
+  Operator &op = *static_cast<Operator *>(pop);
+  CgWork &wk = *static_cast<CgWork *>(pwk);
+  cudaStream_t s = lib_stream();
+  const long n = op.n;
+  double *r = nullptr, *w = nullptr;
+  float *g32 = nullptr, *c32 = nullptr, *r32 = nullptr, *e32 = nullptr,
+        *rr32 = nullptr, *w32 = nullptr, *p32 = nullptr;
+  int st = NB_OK;
+  auto A = [&](void **p, size_t b) {
+    if (st) return;
+    if (cudaMalloc(p, b) != cudaSuccess) st = fail(NB_ERR_CUDA, "nb_cg_mixed: out of memory");
+  };
+  A((void **)&r, n * 8);
+  A((void **)&w, n * 8);
+  A((void **)&g32, 6 * n * 4);
+  A((void **)&c32, n * 4);
+  A((void **)&r32, n * 4);
+  A((void **)&e32, n * 4);
+  A((void **)&rr32, n * 4);
+  A((void **)&w32, n * 4);
+  A((void **)&p32, n * 4);
+  int k = 0, inner = 0;
+  double rn0 = 0.0, rn = 0.0;
+  if (!st) st = vec_convert<float, double>(g32, g, 6 * n, s);
+  if (!st) st = vec_convert<float, double>(c32, c, n, s);
+  // x = 0, r = mask(f)
+  if (!st && cudaMemsetAsync(x, 0, n * 8, s) != cudaSuccess) st = fail(NB_ERR_CUDA, "memset");
+  if (!st) st = vec_copy<double>(r, f, n, s);
+  if (!st) st = vec_mask<double>(r, op.d_mask_list, op.n_mask, s);
+  while (!st) {
+    if (!st) st = vec_glsc3<double>(r, c, r, n, wk, wk.dot_out + 3, nullptr, 0, 0, s);
+    double rr = 0.0;
+    if (!st && cudaMemcpyAsync(&rr, wk.dot_out + 3, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      st = fail(NB_ERR_CUDA, "copy");
+    if (!st && cudaStreamSynchronize(s) != cudaSuccess) st = fail(NB_ERR_CUDA, "sync");
+    if (st) break;
+    rn = std::sqrt(rr);
+    if (k == 0) rn0 = rn;
+    if (rn0 == 0.0 || rn / rn0 <= tol || k >= max_outer) break;
+    // inner FP32 solve of A e = r / |r|
+    st = dev_scale_to_f32(r32, r, 1.0 / rn, n, s);
+    if (!st) st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s);
+    if (!st) st = dev_axpy_f32(x, e32, rn, n, s);
+    // FP64 defect: r = f - A x
+    if (!st) st = apply_ax<double>(op, w, x, g, s);
+    if (!st) st = dev_residual(op, r, f, w, n, s);
+    inner += inner_iters;
+    ++k;
+  }
+  cudaFree(r); cudaFree(w); cudaFree(g32); cudaFree(c32); cudaFree(r32);
+  cudaFree(e32); cudaFree(rr32); cudaFree(w32); cudaFree(p32);
+  if (st) return st;
+  if (outer) *outer = k;
+  if (inner_total) *inner_total = inner;
+  if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
+  return NB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,558 @@
+// nb_solver.cu -- device-resident operator set-up and the CG iteration.
+//
+// One CG iteration of cg.f:48-75 with the identity preconditioner is three
+// kernels and no host round trip:
+//   k_ax (MODE 1)   p = z + beta p; w_L = A_L p per element; interior points
+//                   finished (w = w_L + 0.1 p); interior part of pap
+//   k_gs_fin        jl-order sum over every group of element-boundary points,
+//                   w = sum + 0.1 p, Dirichlet mask, boundary part of pap;
+//                   last block forms pap and alpha
+//   k_cg_update     x += alpha p, r -= alpha w, rtr; last block forms beta
+// CG scalars stay on the device.  The unfused path (element product, jl
+// gather-scatter, add2s2, maskit, glsc3 as separate kernels) covers meshes
+// whose numbering shares element-interior points, and flagged handles.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "nb_solver.h"
+
+namespace nb {
+
+Operator::~Operator() {
+  if (dD) cudaFree(dD);
+  if (fD) cudaFree(fD);
+  gs_release(&gs);
+  if (d_mask_list) cudaFree(d_mask_list);
+  if (d_face) cudaFree(d_face);
+  if (bnd_off) cudaFree(bnd_off);
+  if (bnd_idx) cudaFree(bnd_idx);
+}
+
+CgWork::~CgWork() {
+  double *ps[] = {partial_ax, partial_gs, partial_up, partial_dot, hist, dot_out};
+  for (double *p : ps)
+    if (p) cudaFree(p);
+  if (counters) cudaFree(counters);
+  if (sc) cudaFree(sc);
+}
+
+static int sm_count() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev);
+    if (cached <= 0) cached = 152;
+  }
+  return cached;
+}
+
+int CgWork::ensure(const Operator &op, int niter) {
+  const int gu = int(std::max(1L, std::min<long>(sm_count() * 8L, (op.n + 255) / 256)));
+  const int gg = int(std::max(1L, std::min<long>(sm_count() * 8L, (long(op.nbg) + 255) / 256)));
+  if (!counters) {
+    NB_CUDA(cudaMalloc(&counters, 8 * sizeof(unsigned)));
+    NB_CUDA(cudaMemset(counters, 0, 8 * sizeof(unsigned)));
+    NB_CUDA(cudaMalloc(&sc, sizeof(CgScalars)));
+    NB_CUDA(cudaMemset(sc, 0, sizeof(CgScalars)));
+    NB_CUDA(cudaMalloc(&dot_out, 8 * sizeof(double)));
+  }
+  const int need_ax = std::max(op.nelt, 1);
+  if (need_ax > cap_ax || gu > grid_up || gg > grid_gs) {
+    if (partial_ax) cudaFree(partial_ax);
+    if (partial_gs) cudaFree(partial_gs);
+    if (partial_up) cudaFree(partial_up);
+    if (partial_dot) cudaFree(partial_dot);
+    cap_ax = std::max(need_ax, cap_ax);
+    grid_up = std::max(gu, grid_up);
+    grid_gs = std::max(gg, grid_gs);
+    NB_CUDA(cudaMalloc(&partial_ax, cap_ax * sizeof(double)));
+    NB_CUDA(cudaMalloc(&partial_gs, grid_gs * sizeof(double)));
+    NB_CUDA(cudaMalloc(&partial_up, grid_up * sizeof(double)));
+    NB_CUDA(cudaMalloc(&partial_dot, grid_up * sizeof(double)));
+  }
+  grid_up = gu;
+  grid_gs = gg;
+  if (niter + 1 > hist_len) {
+    if (hist) cudaFree(hist);
+    hist_len = niter + 1;
+    NB_CUDA(cudaMalloc(&hist, 5 * sizeof(double) * hist_len));
+  }
+  return NB_OK;
+}
+
+// ------------------------------------------------------------ set-up --
+static bool is_elem_boundary(long pt, int lx) {
+  const long l3 = long(lx) * lx * lx;
+  const int r = int(pt % l3);
+  const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+  return i == 0 || i == lx - 1 || j == 0 || j == lx - 1 || k == 0 || k == lx - 1;
+}
+
+// Groups of element-boundary points for the fused pass: every gather-scatter
+// group (all members must be element-boundary points) and every boundary
+// point that belongs to no group, in order of the first member.
+static void build_boundary_groups(Operator *op) {
+  op->fused_ok = false;
+  op->bnd_off_h.clear();
+  op->bnd_idx_h.clear();
+  if (!op->gs.symmetric) return;
+  const long n = op->n;
+  std::vector<int> grp(n, -1);  // >=0 group id at its primary, -2 member
+  std::vector<int> goff;
+  std::vector<int> gmem;
+  {
+    const uint32_t END = uint32_t(-1);
+    const std::vector<uint32_t> &m = op->gsh_host.map[1];
+    size_t q = 0;
+    while (q < m.size() && m[q] != END) {
+      const int g = int(goff.size());
+      goff.push_back(int(gmem.size()));
+      grp[m[q]] = g;
+      gmem.push_back(int(m[q++]));
+      while (m[q] != END) {
+        grp[m[q]] = -2;
+        gmem.push_back(int(m[q++]));
+      }
+      ++q;
+    }
+    goff.push_back(int(gmem.size()));
+  }
+  for (long pt = 0; pt < n; ++pt) {
+    const bool b = is_elem_boundary(pt, op->lx);
+    if (!b) {
+      if (grp[pt] != -1) return;  // an interior point is shared
+      continue;
+    }
+    if (grp[pt] == -2) continue;
+    op->bnd_off_h.push_back(int(op->bnd_idx_h.size()));
+    if (grp[pt] >= 0) {
+      const int g = grp[pt];
+      for (int q = goff[g]; q < goff[g + 1]; ++q) op->bnd_idx_h.push_back(unsigned(gmem[q]));
+    } else {
+      op->bnd_idx_h.push_back(unsigned(pt));
+    }
+  }
+  op->bnd_off_h.push_back(int(op->bnd_idx_h.size()));
+  op->nbg = int(op->bnd_off_h.size()) - 1;
+  op->fused_ok = n < (1L << 31);
+}
+
+std::vector<int> full_mask_list(const Operator &op) {
+  std::vector<int> list;
+  const int lx = op.lx;
+  const long l3 = long(lx) * lx * lx;
+  for (int e = 0; e < op.nelt; ++e) {
+    const unsigned f = op.face[e];
+    if (!f) continue;
+    for (int k = 0; k < lx; ++k)
+      for (int j = 0; j < lx; ++j)
+        for (int i = 0; i < lx; ++i) {
+          const bool m = ((f & 1u) && i == 0) || ((f & 2u) && i == lx - 1) ||
+                         ((f & 4u) && j == 0) || ((f & 8u) && j == lx - 1) ||
+                         ((f & 16u) && k == 0) || ((f & 32u) && k == lx - 1);
+          if (m) list.push_back(int(l3 * e + i + lx * j + lx * lx * k));
+        }
+  }
+  return list;
+}
+
+int operator_set_mask(Operator *op, const std::vector<int> &list_in) {
+  std::vector<int> list = list_in;
+  std::sort(list.begin(), list.end());
+  list.erase(std::unique(list.begin(), list.end()), list.end());
+  op->mask_list = list;
+  if (op->d_mask_list) cudaFree(op->d_mask_list);
+  op->d_mask_list = nullptr;
+  op->n_mask = int(list.size());
+  if (!list.empty()) {
+    NB_CUDA(cudaMalloc(&op->d_mask_list, list.size() * sizeof(int)));
+    NB_CUDA(cudaMemcpy(op->d_mask_list, list.data(), list.size() * sizeof(int),
+                       cudaMemcpyHostToDevice));
+  }
+  if (op->nbg > 0 && !op->bnd_idx_h.empty()) {
+    for (int v : list)
+      if (!is_elem_boundary(v, op->lx)) op->fused_ok = false;
+    std::vector<unsigned char> masked(op->n, 0);
+    for (int v : list) masked[v] = 1;
+    std::vector<unsigned> idx = op->bnd_idx_h;
+    for (auto &v : idx)
+      if (masked[v]) v |= 0x80000000u;
+    if (!op->bnd_idx) {
+      NB_CUDA(cudaMalloc(&op->bnd_idx, idx.size() * sizeof(unsigned)));
+      NB_CUDA(cudaMalloc(&op->bnd_off, op->bnd_off_h.size() * sizeof(int)));
+      NB_CUDA(cudaMemcpy(op->bnd_off, op->bnd_off_h.data(),
+                         op->bnd_off_h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+    NB_CUDA(cudaMemcpy(op->bnd_idx, idx.data(), idx.size() * sizeof(unsigned),
+                       cudaMemcpyHostToDevice));
+  }
+  return NB_OK;
+}
+
+int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
+                  const int *lglel, const double *dxm1, const GsHost &maps,
+                  int mask_mode, cudaStream_t s) {
+  if (lx < 2 || lx > kMaxLx)
+    return fail(NB_ERR_UNSUPPORTED, "lx1=%d outside the supported range 2..%d", lx, kMaxLx);
+  if (nelt <= 0) return fail(NB_ERR_ARG, "nelt=%d must be positive", nelt);
+  op->nelx = nelx;
+  op->nely = nely;
+  op->nelz = nelz;
+  op->nelt = nelt;
+  op->lx = lx;
+  op->n = long(nelt) * lx * lx * lx;
+  op->stream = s;
+  op->lglel.assign(lglel, lglel + nelt);
+  op->D.assign(dxm1, dxm1 + lx * lx);
+  op->mask_mode = mask_mode;
+  NB_CUDA(cudaMalloc(&op->dD, lx * lx * sizeof(double)));
+  NB_CUDA(cudaMalloc(&op->fD, lx * lx * sizeof(float)));
+  std::vector<float> fDh(op->D.begin(), op->D.end());
+  NB_CUDA(cudaMemcpy(op->dD, op->D.data(), lx * lx * sizeof(double), cudaMemcpyHostToDevice));
+  NB_CUDA(cudaMemcpy(op->fD, fDh.data(), lx * lx * sizeof(float), cudaMemcpyHostToDevice));
+  op->gsh_host = maps;
+  NB_TRY(gs_upload(op->gsh_host, int(op->n), &op->gs, s));
+  op->face.resize(nelt);
+  for (int e = 0; e < nelt; ++e)
+    op->face[e] = (unsigned char)face_bits(op->lglel[e], nelx, nely, nelz);
+  NB_CUDA(cudaMalloc(&op->d_face, nelt));
+  NB_CUDA(cudaMemcpy(op->d_face, op->face.data(), nelt, cudaMemcpyHostToDevice));
+  build_boundary_groups(op);
+  op->mask_built = false;
+  if (mask_mode == 1) {
+    op->mask_built = true;
+    NB_TRY(operator_set_mask(op, full_mask_list(*op)));
+  } else {
+    NB_TRY(operator_set_mask(op, std::vector<int>()));
+  }
+  return NB_OK;
+}
+
+int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
+                 int mask_mode, cudaStream_t s) {
+  if (nelx <= 0 || nely <= 0 || nelz <= 0)
+    return fail(NB_ERR_ARG, "box %dx%dx%d must be positive", nelx, nely, nelz);
+  const long nelt = long(nelx) * nely * nelz;
+  if (nelt * lx * lx * lx >= (1L << 31))
+    return fail(NB_ERR_UNSUPPORTED, "n = nelt*lx1^3 = %ld exceeds 2^31-1",
+                nelt * lx * lx * lx);
+  std::vector<int> lglel(nelt);
+  for (long e = 0; e < nelt; ++e) lglel[e] = int(e + 1);  // brick, np=1
+  std::vector<double> a(lx * lx), b(lx), c(lx * lx), d(lx * lx), z(lx);
+  semhat(a.data(), b.data(), c.data(), d.data(), z.data(), lx - 1);
+  const long n = nelt * lx * lx * lx;
+  std::vector<int64_t> glo(n);
+  set_vert_box(glo.data(), lx, int(nelt), nelx, nely, lglel.data());
+  GsHost maps;
+  gs_topology(glo.data(), int(n), &maps);
+  return operator_from(op, nelx, nely, nelz, int(nelt), lx, lglel.data(),
+                       d.data(), maps, mask_mode, s);
+}
+
+// ------------------------------------------------------- vector kernels --
+namespace {
+
+template <typename T>
+__global__ void k_add2s1(T *a, const T *b, const double *c1d, double c1h, long n) {
+  const T c1 = T(c1d ? *c1d : c1h);
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = fma_rn(c1, a[q], b[q]);
+}
+template <typename T>
+__global__ void k_add2s2(T *a, const T *b, T c1, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = fma_rn(c1, b[q], a[q]);
+}
+template <typename T>
+__global__ void k_copy_first(T *p, const T *z, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    p[q] = z[q];
+}
+template <typename T, typename S>
+__global__ void k_convert(T *a, const S *b, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = T(b[q]);
+}
+template <typename T>
+__global__ void k_mask_list(T *w, const int *list, int nlist) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nlist) w[list[q]] = T(0);
+}
+// zero every element's domain faces (the build branch of maskit, cg.f:236-250)
+template <typename T>
+__global__ void k_mask_faces(T *w, const unsigned char *face, int lx, long n) {
+  const long l3 = long(lx) * lx * lx;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    const unsigned f = face[q / l3];
+    if (!f) continue;
+    const int r = int(q % l3);
+    const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+    if (((f & 1u) && i == 0) || ((f & 2u) && i == lx - 1) || ((f & 4u) && j == 0) ||
+        ((f & 8u) && j == lx - 1) || ((f & 16u) && k == 0) || ((f & 32u) && k == lx - 1))
+      w[q] = T(0);
+  }
+}
+// pap = glsc3(w,c,p), alpha = rtz1/pap (unfused path)
+__global__ void k_set_alpha(CgScalars *sc, const double *pap) {
+  sc->pap = *pap;
+  sc->alpha = sc->rtz1 / *pap;
+}
+
+int grid_for(long n) {
+  return int(std::max(1L, std::min<long>(long(sm_count()) * 8, (n + 255) / 256)));
+}
+
+}  // namespace
+
+template <typename T>
+int vec_add2s1(T *a, const T *b, const double *c1d, double c1, long n, cudaStream_t s) {
+  k_add2s1<T><<<grid_for(n), 256, 0, s>>>(a, b, c1d, c1, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+template <typename T>
+int vec_add2s2(T *a, const T *b, double c1, long n, cudaStream_t s) {
+  k_add2s2<T><<<grid_for(n), 256, 0, s>>>(a, b, T(c1), n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+template <typename T>
+int vec_mask(T *w, const int *list, int nlist, cudaStream_t s) {
+  if (nlist <= 0) return NB_OK;
+  k_mask_list<T><<<(nlist + 255) / 256, 256, 0, s>>>(w, list, nlist);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+template <typename T>
+int vec_copy(T *a, const T *b, long n, cudaStream_t s) {
+  NB_CUDA(cudaMemcpyAsync(a, b, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  return NB_OK;
+}
+template <typename T, typename S>
+int vec_convert(T *a, const S *b, long n, cudaStream_t s) {
+  k_convert<T, S><<<grid_for(n), 256, 0, s>>>(a, b, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+template <typename T>
+int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
+              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s) {
+  const int gr = std::min(grid_for(n), wk.grid_up);
+  k_glsc3<T><<<gr, 256, 0, s>>>(a, b, m, n, wk.partial_dot, wk.counters + 2, out,
+                                sc, mode, wk.hist, iter);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+template int vec_add2s1<double>(double *, const double *, const double *, double, long, cudaStream_t);
+template int vec_add2s1<float>(float *, const float *, const double *, double, long, cudaStream_t);
+template int vec_add2s2<double>(double *, const double *, double, long, cudaStream_t);
+template int vec_add2s2<float>(float *, const float *, double, long, cudaStream_t);
+template int vec_mask<double>(double *, const int *, int, cudaStream_t);
+template int vec_mask<float>(float *, const int *, int, cudaStream_t);
+template int vec_copy<double>(double *, const double *, long, cudaStream_t);
+template int vec_copy<float>(float *, const float *, long, cudaStream_t);
+template int vec_convert<float, double>(float *, const double *, long, cudaStream_t);
+template int vec_convert<double, float>(double *, const float *, long, cudaStream_t);
+template int vec_glsc3<double>(const double *, const double *, const double *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t);
+template int vec_glsc3<float>(const float *, const float *, const float *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t);
+
+// ------------------------------------------------------------ ax launch --
+namespace {
+template <typename T, int LX, int MODE>
+int launch_ax_lx(AxArgs<T> a, cudaStream_t s) {
+  const size_t sm = ax_smem_bytes<T, LX>();
+  static bool attr_set = false;
+  if (!attr_set) {
+    NB_CUDA(cudaFuncSetAttribute(k_ax<T, LX, MODE>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    attr_set = true;
+  }
+  k_ax<T, LX, MODE><<<a.nelt, dim3(LX, LX), sm, s>>>(a);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+template <typename T, int MODE>
+int launch_ax_mode(int lx, AxArgs<T> a, cudaStream_t s) {
+  switch (lx) {
+#define NB_CASE(L) case L: return launch_ax_lx<T, L, MODE>(a, s);
+    NB_CASE(2) NB_CASE(3) NB_CASE(4) NB_CASE(5) NB_CASE(6) NB_CASE(7)
+    NB_CASE(8) NB_CASE(9) NB_CASE(10) NB_CASE(11) NB_CASE(12) NB_CASE(13)
+    NB_CASE(14) NB_CASE(15) NB_CASE(16)
+#undef NB_CASE
+    default:
+      return fail(NB_ERR_UNSUPPORTED, "ax: lx1=%d not supported (2..%d)", lx, kMaxLx);
+  }
+}
+}  // namespace
+
+template <typename T>
+int launch_ax(const Operator &op, int mode, AxArgs<T> a, cudaStream_t s) {
+  a.nelt = op.nelt;
+  if (mode == 0) return launch_ax_mode<T, 0>(op.lx, a, s);
+  return launch_ax_mode<T, 1>(op.lx, a, s);
+}
+template int launch_ax<double>(const Operator &, int, AxArgs<double>, cudaStream_t);
+template int launch_ax<float>(const Operator &, int, AxArgs<float>, cudaStream_t);
+
+// maskit (cg.f:214-258) on a device vector: the build branch (zero every
+// element's domain faces, then record element 1's zero entries) on the first
+// call after a reset in reference mode, the recorded list otherwise.
+template <typename T>
+static int maskit_dev(Operator &op, T *w, cudaStream_t s) {
+  if (op.mask_mode == 0 && !op.mask_built) {
+    k_mask_faces<T><<<grid_for(op.n), 256, 0, s>>>(w, op.d_face, op.lx, op.n);
+    NB_CUDA(cudaGetLastError());
+    const int l3 = op.lx * op.lx * op.lx;
+    std::vector<T> e1(l3);
+    NB_CUDA(cudaMemcpyAsync(e1.data(), w, l3 * sizeof(T), cudaMemcpyDeviceToHost, s));
+    NB_CUDA(cudaStreamSynchronize(s));
+    std::vector<int> list;
+    for (int i = 0; i < l3; ++i)
+      if (e1[i] == T(0)) list.push_back(i);
+    op.mask_built = true;
+    return operator_set_mask(&op, list);
+  }
+  return vec_mask<T>(w, op.d_mask_list, op.n_mask, s);
+}
+
+template <typename T>
+int apply_ax(const Operator &op_c, T *w, const T *u, const T *g, cudaStream_t s) {
+  Operator &op = const_cast<Operator &>(op_c);
+  AxArgs<T> a{};
+  a.w = w;
+  a.u = u;
+  a.g = g;
+  a.D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
+  NB_TRY(launch_ax<T>(op, 0, a, s));
+  NB_TRY(gs_exec(op.gs, w, std::is_same<T, double>::value ? 1 : 2, 1, 0, s));
+  NB_TRY(vec_add2s2<T>(w, u, 0.1, op.n, s));
+  return maskit_dev<T>(op, w, s);
+}
+template int apply_ax<double>(const Operator &, double *, const double *, const double *, cudaStream_t);
+template int apply_ax<float>(const Operator &, float *, const float *, const float *, cudaStream_t);
+
+// ------------------------------------------------------------------ CG --
+// cg.f:36-42: x = 0, r = mask(f), rnorm = sqrt(glsc3(r,c,r)).
+template <typename T>
+static int cg_begin_t(Operator &op, CgWork &wk, T *x, const T *f, const T *c,
+                      T *r, bool zero_x, int niter, cudaStream_t s) {
+  const long n = op.n;
+  NB_TRY(wk.ensure(op, niter));
+  if (zero_x) NB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));  // rzero(x)
+  NB_TRY(vec_copy<T>(r, f, n, s));                                 // copy(r,f)
+  NB_TRY(maskit_dev<T>(op, r, s));
+  return vec_glsc3<T>(r, c, r, n, wk, wk.dot_out, wk.sc, 1, 0, s);
+}
+
+// iterations it0..it1 of cg.f:48-75
+template <typename T>
+static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
+                      T *r, T *w, T *p, T *z, int it0, int it1, int niter,
+                      Precond *M, bool force_unfused, cudaStream_t s) {
+  const long n = op.n;
+  const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
+  const bool fused = op.fused_ok && !force_unfused;
+  for (int iter = it0; iter <= it1; ++iter) {
+    T *zz = r;
+    if (M) {
+      if (!std::is_same<T, double>::value)
+        return fail(NB_ERR_UNSUPPORTED, "preconditioned CG is FP64 only");
+      NB_TRY(M->apply((double *)z, (double *)r, s));
+      zz = z;
+      NB_TRY(vec_glsc3<T>(r, c, z, n, wk, wk.dot_out + 1, wk.sc, 2, iter, s));
+    } else if (z && z != r && iter == niter) {
+      // hsmg_dum's solveM leaves z = r of the last iteration (hsmg_dum.f:9-14)
+      NB_TRY(vec_copy<T>(z, r, n, s));
+    }
+    if (fused) {
+      AxArgs<T> a{};
+      a.w = w;
+      a.u = zz;
+      a.p = p;
+      a.g = g;
+      a.c = c;
+      a.D = D;
+      a.sc = wk.sc;
+      a.partial = wk.partial_ax;
+      a.first = iter == 1;
+      NB_TRY(launch_ax<T>(op, 1, a, s));
+      k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx,
+                                             op.nbg, wk.partial_gs, wk.partial_ax,
+                                             op.nelt, wk.counters + 0, wk.sc);
+      NB_CUDA(cudaGetLastError());
+    } else {
+      if (iter == 1)
+        k_copy_first<T><<<grid_for(n), 256, 0, s>>>(p, zz, n);
+      else
+        NB_TRY(vec_add2s1<T>(p, zz, &wk.sc->beta, 0.0, n, s));
+      NB_TRY(apply_ax<T>(op, w, p, g, s));
+      NB_TRY(vec_glsc3<T>(w, c, p, n, wk, wk.dot_out + 2, nullptr, 0, iter, s));
+      k_set_alpha<<<1, 1, 0, s>>>(wk.sc, wk.dot_out + 2);
+      NB_CUDA(cudaGetLastError());
+    }
+    k_cg_update<T><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, n, wk.partial_up,
+                                              wk.counters + 1, wk.sc,
+                                              iter < wk.hist_len ? wk.hist : nullptr,
+                                              iter, M == nullptr);
+    NB_CUDA(cudaGetLastError());
+  }
+  return NB_OK;
+}
+
+int launch_gs_fin(const Operator &op, CgWork &wk, double *w, const double *p,
+                  const double *c, cudaStream_t s) {
+  k_gs_fin<double><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx,
+                                              op.nbg, wk.partial_gs, wk.partial_ax,
+                                              op.nelt, wk.counters + 0, wk.sc);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+int launch_cg_update(const Operator &op, CgWork &wk, double *x, double *r,
+                     const double *p, const double *w, const double *c,
+                     int iter, cudaStream_t s) {
+  k_cg_update<double><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, op.n, wk.partial_up,
+                                                 wk.counters + 1, wk.sc, nullptr,
+                                                 iter, 1);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+int cg_device(Operator &op, CgWork &wk, double *x, const double *f,
+              const double *g, const double *c, double *r, double *w,
+              double *p, double *z, int niter, Precond *M, bool force_unfused,
+              cudaStream_t s) {
+  NB_TRY(cg_begin_t<double>(op, wk, x, f, c, r, true, niter, s));
+  return cg_steps_t<double>(op, wk, x, g, c, r, w, p, z, 1, niter, niter, M,
+                            force_unfused, s);
+}
+
+int cg_begin(Operator &op, CgWork &wk, double *x, const double *f,
+             const double *c, double *r, int niter, cudaStream_t s) {
+  return cg_begin_t<double>(op, wk, x, f, c, r, true, niter, s);
+}
+
+int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
+             const double *c, double *r, double *w, double *p, int it0,
+             int it1, cudaStream_t s) {
+  return cg_steps_t<double>(op, wk, x, g, c, r, w, p, r, it0, it1, -1, nullptr,
+                            false, s);
+}
+
+int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
+                  const float *g, const float *c, float *r, float *w, float *p,
+                  int niter, cudaStream_t s) {
+  NB_TRY(cg_begin_t<float>(op, wk, x, f, c, r, true, niter, s));
+  return cg_steps_t<float>(op, wk, x, g, c, r, w, p, r, 1, niter, niter,
+                           nullptr, false, s);
+}
+
+}  // namespace nb

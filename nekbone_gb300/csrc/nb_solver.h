@@ -1,0 +1,121 @@
+// nb_solver.h -- device-resident operator and CG solver state.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "nb_internal.h"
+#include "nb_kernels.cuh"
+
+namespace nb {
+
+// A mesh with its gather-scatter topology, the derivative matrix and the
+// Dirichlet mask, all resident on the device.
+struct Operator {
+  int nelx = 0, nely = 0, nelz = 0, nelt = 0, lx = 0;
+  long n = 0;
+  std::vector<int> lglel;          // global element numbers (1-based)
+  std::vector<double> D;           // dxm1, column-major
+  double *dD = nullptr;
+  float *fD = nullptr;
+  GsHost gsh_host;                 // jl maps of the dssum handle
+  GsDevice gs;                     // device form
+  // mask state (maskit, cg.f:214-258)
+  int mask_mode = 1;               // 0 reference list semantics, 1 full
+  bool mask_built = false;         // reference mode: list built
+  std::vector<int> mask_list;      // masked local indices (deduplicated)
+  int *d_mask_list = nullptr;
+  int n_mask = 0;
+  std::vector<unsigned char> face;  // per-element domain faces (get_face)
+  unsigned char *d_face = nullptr;
+  // fused gather-scatter over element boundary points
+  bool fused_ok = false;
+  int nbg = 0;
+  std::vector<int> bnd_off_h;
+  std::vector<unsigned> bnd_idx_h;  // without mask flags
+  int *bnd_off = nullptr;
+  unsigned *bnd_idx = nullptr;      // with mask flags in bit 31
+  cudaStream_t stream = nullptr;
+
+  ~Operator();
+};
+
+// Work space of one CG solve (reduction partials, scalars, history).
+struct CgWork {
+  double *partial_ax = nullptr, *partial_gs = nullptr, *partial_up = nullptr,
+         *partial_dot = nullptr;
+  unsigned *counters = nullptr;  // [0] gs_fin, [1] update, [2] glsc3
+  CgScalars *sc = nullptr;
+  double *hist = nullptr;
+  int hist_len = 0;
+  double *dot_out = nullptr;
+  int grid_up = 0, grid_gs = 0, cap_ax = 0;
+  ~CgWork();
+  int ensure(const Operator &op, int niter);
+};
+
+// Builds the operator for a box of nelx*nely*nelz elements with lx points
+// per direction on the reference's brick decomposition (init_mesh,
+// driver.f:117-194) and numbering (set_vert_box, prox_dssum.f:42-73).
+int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
+                 int mask_mode, cudaStream_t s);
+// Operator from a caller's mesh description and existing jl maps.
+int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt,
+                  int lx, const int *lglel, const double *dxm1,
+                  const GsHost &maps, int mask_mode, cudaStream_t s);
+// Re-derives the device mask list and the fused-path mask flags.
+int operator_set_mask(Operator *op, const std::vector<int> &list);
+// Full Dirichlet mask of every element's domain faces (get_face per element).
+std::vector<int> full_mask_list(const Operator &op);
+
+// ------------------------------------------------------------- kernels --
+template <typename T>
+int launch_ax(const Operator &op, int mode, AxArgs<T> a, cudaStream_t s);
+template <typename T>
+int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
+              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s);
+template <typename T>
+int vec_add2s1(T *a, const T *b, const double *c1_dev, double c1, long n,
+               cudaStream_t s);
+template <typename T>
+int vec_add2s2(T *a, const T *b, double c1, long n, cudaStream_t s);
+template <typename T>
+int vec_mask(T *w, const int *list, int nlist, cudaStream_t s);
+template <typename T>
+int vec_copy(T *a, const T *b, long n, cudaStream_t s);
+template <typename T, typename S>
+int vec_convert(T *a, const S *b, long n, cudaStream_t s);
+
+// w = mask(QQ^T A_L u + 0.1 u)  (ax, cg.f:96-125), unfused path.
+template <typename T>
+int apply_ax(const Operator &op, T *w, const T *u, const T *g, cudaStream_t s);
+
+// CG of cg.f:2-84 on device data.  z may equal r (identity preconditioner).
+// precond: nullptr for the identity (hsmg_dum.f), else z = M^-1 r.
+struct Precond {
+  virtual int apply(double *z, double *r, cudaStream_t s) = 0;
+  virtual ~Precond() {}
+};
+int cg_device(Operator &op, CgWork &wk, double *x, const double *f,
+              const double *g, const double *c, double *r, double *w,
+              double *p, double *z, int niter, Precond *M, bool force_unfused,
+              cudaStream_t s);
+// The same iteration split in two: the set-up of cg.f:36-42, then
+// iterations it0..it1 (identity preconditioner), scalars kept on the device.
+int cg_begin(Operator &op, CgWork &wk, double *x, const double *f,
+             const double *c, double *r, int niter, cudaStream_t s);
+int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
+             const double *c, double *r, double *w, double *p, int it0,
+             int it1, cudaStream_t s);
+// the second and third kernels of a fused FP64 iteration, for timing
+int launch_gs_fin(const Operator &op, CgWork &wk, double *w, const double *p,
+                  const double *c, cudaStream_t s);
+int launch_cg_update(const Operator &op, CgWork &wk, double *x, double *r,
+                     const double *p, const double *w, const double *c,
+                     int iter, cudaStream_t s);
+// FP32 variant (inner solves of the mixed-precision path), x starts at 0.
+int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
+                  const float *g, const float *c, float *r, float *w, float *p,
+                  int niter, cudaStream_t s);
+
+}  // namespace nb
