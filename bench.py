@@ -57,7 +57,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-sample-nel", type=int, default=16)
-    ap.add_argument("--cpu-sample-iters", type=int, default=10)
+    ap.add_argument("--cpu-sample-iters", type=int, default=100)
     return ap.parse_args()
 
 

@@ -24,7 +24,12 @@ BUILD = PKG / "_build"
 LIB = PKG / "libnekbone_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code is built without floating-point contraction so that the set-up
+# math (GLL points, derivative matrices, multigrid operators) rounds the same
+# way on x86-64 and aarch64 (gcc contracts a*b+c into fma by default on
+# aarch64).  Device code spells every fused multiply-add out explicitly.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
