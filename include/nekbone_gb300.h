@@ -184,6 +184,21 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
               const double *c, double tol, int max_iter, int check_every,
               int *iters, double *relres);
 
+/* glsc3 on device vectors that allocates nothing -- no counterpart in the
+ * reference.  For callers that cannot call cudaMalloc while they run: codes
+ * whose device memory belongs to their own pool (an OpenACC or CUDA Fortran
+ * host), or loops that must not pay cudaMalloc's implicit device
+ * synchronisation.  a, b, mult: device vectors of length n; result: one
+ * device double, written asynchronously on stream (a cudaStream_t, NULL =
+ * the legacy default stream).  The reduction's partial sums live in a fixed
+ * device array of the library (about 128 KiB per GPU that loads it, held
+ * until exit), so n must not exceed NB_NOALLOC_MAX_N.  Calls share that
+ * array: calls that overlap on the GPU race.  The first call on a device
+ * looks the array up; make it before any stream capture. */
+#define NB_NOALLOC_MAX_N 67108864L
+int nb_glsc3_noalloc(const double *a, const double *b, const double *mult,
+                     long n, double *result, void *stream);
+
 /* Synchronise the library's stream. */
 int nb_sync(void);
 /* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for

@@ -47,7 +47,7 @@ EXPORTS = (
     "nb_mesh_destroy", "nb_mesh_npts", "nb_mesh_info", "nb_setup_g",
     "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
     "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync", "nb_stream",
-    "nb_time_cg_kernels",
+    "nb_time_cg_kernels", "nb_glsc3_noalloc",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -73,6 +73,10 @@ lib.nb_mesh_info.argtypes = [_p, _p, _p, _p]
 lib.nb_stream.restype = _p
 lib.nb_time_cg_kernels.restype = _i
 lib.nb_time_cg_kernels.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
+lib.nb_glsc3_noalloc.restype = _i
+lib.nb_glsc3_noalloc.argtypes = [_p, _p, _p, _l, _p, _p]
+#: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
+NOALLOC_MAX_N = 67108864
 
 # return-status error mode for Python callers: errors raise NekboneError
 lib.nekbone_set_error_mode(1)
