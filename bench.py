@@ -239,6 +239,21 @@ def run_ours(a, rank, world, local):
                 "kernel_ms": {"ax": kms[0], "gs_fin": kms[1], "update": kms[2]},
                 "fp64_tflops": flops_pt * n / (kms[0] * 1e-3) / 1e12}
 
+    # the FP32 iteration of the mixed solver's inner CG, same mesh
+    f32, g32, c32 = f.float(), g.float(), c.float()
+    x32, r32, w32, p32 = (torch.zeros(n, dtype=torch.float32, device=dev) for _ in range(4))
+    torch.cuda.synchronize()
+    kms32 = mesh.time_cg_kernels_f32(x32.data_ptr(), f32.data_ptr(), g32.data_ptr(),
+                                     c32.data_ptr(), r32.data_ptr(), w32.data_ptr(),
+                                     p32.data_ptr(), reps=10)
+    ax32_bytes = 32 * n
+    roofline["fp32_inner_iteration"] = {
+        "kernel_ms": {"ax": kms32[0], "gs_fin": kms32[1], "update": kms32[2]},
+        "ax_achieved_gbs": ax32_bytes / (kms32[0] * 1e-3) / 1e9,
+        "ax_frac": ax32_bytes / (kms32[0] * 1e-3) / 1e9 / peak,
+        "iteration_ms": float(sum(kms32))}
+    del f32, g32, c32, x32, r32, w32, p32
+
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
            "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",

@@ -212,6 +212,11 @@ void *nb_stream(void);
 int nb_time_cg_kernels(nb_mesh *mesh, double *x, const double *f,
                        const double *g, const double *c, double *r, double *w,
                        double *p, int reps, double *ms3);
+/* The same for the FP32 iteration of the mixed solver's inner CG (float
+ * device vectors, g as 6n floats). */
+int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
+                           const float *g, const float *c, float *r, float *w,
+                           float *p, int reps, double *ms3);
 
 #ifdef __cplusplus
 }

@@ -47,7 +47,7 @@ EXPORTS = (
     "nb_mesh_destroy", "nb_mesh_npts", "nb_mesh_info", "nb_setup_g",
     "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
     "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync", "nb_stream",
-    "nb_time_cg_kernels", "nb_glsc3_noalloc",
+    "nb_time_cg_kernels", "nb_glsc3_noalloc", "nb_time_cg_kernels_f32",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -73,6 +73,8 @@ lib.nb_mesh_info.argtypes = [_p, _p, _p, _p]
 lib.nb_stream.restype = _p
 lib.nb_time_cg_kernels.restype = _i
 lib.nb_time_cg_kernels.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
+lib.nb_time_cg_kernels_f32.restype = _i
+lib.nb_time_cg_kernels_f32.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
 lib.nb_glsc3_noalloc.restype = _i
 lib.nb_glsc3_noalloc.argtypes = [_p, _p, _p, _l, _p, _p]
 #: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
@@ -387,6 +389,12 @@ class DeviceMesh:
         ms = _np.zeros(3)
         _check(lib.nb_time_cg_kernels(self._h, _p(x), _p(f), _p(g), _p(c), _p(r), _p(w),
                                       _p(p), reps, _ptr(ms)))
+        return ms
+
+    def time_cg_kernels_f32(self, x, f, g, c, r, w, p, reps: int = 10):
+        ms = _np.zeros(3)
+        _check(lib.nb_time_cg_kernels_f32(self._h, _p(x), _p(f), _p(g), _p(c), _p(r),
+                                          _p(w), _p(p), reps, _ptr(ms)))
         return ms
 
     def cg_tol(self, x, f, g, c, tol: float, max_iter: int = 20000, check_every: int = 25):

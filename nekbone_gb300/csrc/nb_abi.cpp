@@ -802,42 +802,18 @@ int nb_time_cg_kernels(nb_mesh *mesh, double *x, const double *f,
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
   if (!mesh->op.fused_ok) return fail(NB_ERR_UNSUPPORTED, "mesh has no fused path");
-  cudaStream_t s = lib_stream();
-  Operator &op = mesh->op;
-  CgWork &wk = mesh->wk;
-  NB_TRY(cg_begin(op, wk, x, f, c, r, reps + 1, s));
-  NB_TRY(cg_steps(op, wk, x, g, c, r, w, p, 1, 1, s));  // sets beta, p
-  cudaEvent_t ev[4];
-  for (auto &e : ev) NB_CUDA(cudaEventCreate(&e));
-  double acc[3] = {0, 0, 0};
-  for (int it = 0; it < reps; ++it) {
-    AxArgs<double> a{};
-    a.w = w;
-    a.u = r;
-    a.p = p;
-    a.g = g;
-    a.c = c;
-    a.D = op.dD;
-    a.sc = wk.sc;
-    a.partial = wk.partial_ax;
-    a.first = 0;
-    NB_CUDA(cudaEventRecord(ev[0], s));
-    NB_TRY(launch_ax<double>(op, 1, a, s));
-    NB_CUDA(cudaEventRecord(ev[1], s));
-    NB_TRY(launch_gs_fin(op, wk, w, p, c, s));
-    NB_CUDA(cudaEventRecord(ev[2], s));
-    NB_TRY(launch_cg_update(op, wk, x, r, p, w, c, it + 2, s));
-    NB_CUDA(cudaEventRecord(ev[3], s));
-    NB_CUDA(cudaEventSynchronize(ev[3]));
-    for (int k = 0; k < 3; ++k) {
-      float ms = 0;
-      NB_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
-      acc[k] += ms;
-    }
-  }
-  for (auto &e : ev) cudaEventDestroy(e);
-  for (int k = 0; k < 3; ++k) ms3[k] = acc[k] / (reps > 0 ? reps : 1);
-  return NB_OK;
+  return time_cg_kernels_t<double>(mesh->op, mesh->wk, x, f, g, c, r, w, p, reps,
+                                   ms3, lib_stream());
+}
+
+int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
+                           const float *g, const float *c, float *r, float *w,
+                           float *p, int reps, double *ms3) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (!mesh->op.fused_ok) return fail(NB_ERR_UNSUPPORTED, "mesh has no fused path");
+  return time_cg_kernels_t<float>(mesh->op, mesh->wk, x, f, g, c, r, w, p, reps,
+                                  ms3, lib_stream());
 }
 
 int nb_sync(void) {

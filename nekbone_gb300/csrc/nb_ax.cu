@@ -1,0 +1,29 @@
+// nb_ax.cu -- launch_ax<T>: the element operator for a mesh and mode.
+#include "nb_solver.h"
+
+namespace nb {
+
+int launch_ax_f64_m0(int lx, AxArgs<double> a, cudaStream_t s);
+int launch_ax_f64_m1(int lx, AxArgs<double> a, cudaStream_t s);
+int launch_ax_f64_m2(int lx, AxArgs<double> a, cudaStream_t s);
+int launch_ax_f32_m0(int lx, AxArgs<float> a, cudaStream_t s);
+int launch_ax_f32_m1(int lx, AxArgs<float> a, cudaStream_t s);
+int launch_ax_f32_m2(int lx, AxArgs<float> a, cudaStream_t s);
+
+template <>
+int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
+  a.nelt = op.nelt;
+  if (mode == 0) return launch_ax_f64_m0(op.lx, a, s);
+  if (mode == 1) return launch_ax_f64_m1(op.lx, a, s);
+  return launch_ax_f64_m2(op.lx, a, s);
+}
+
+template <>
+int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
+  a.nelt = op.nelt;
+  if (mode == 0) return launch_ax_f32_m0(op.lx, a, s);
+  if (mode == 1) return launch_ax_f32_m1(op.lx, a, s);
+  return launch_ax_f32_m2(op.lx, a, s);
+}
+
+}  // namespace nb

@@ -1,0 +1,8 @@
+// Element operator instantiations: double, mode 0 (see nb_kernels.cuh).
+#include "nb_ax_launch.cuh"
+
+namespace nb {
+int launch_ax_f64_m0(int lx, AxArgs<double> a, cudaStream_t s) {
+  return launch_ax_mode<double, 0>(lx, a, s);
+}
+}  // namespace nb

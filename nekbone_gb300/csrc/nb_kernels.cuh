@@ -88,33 +88,75 @@ struct CgScalars {
 //         masked) are finished here: w = w_L + 0.1 p (ax, cg.f:119); element
 //         boundary points keep w_L for the gather-scatter pass; the interior
 //         part of pap = glsc3(w,c,p) goes to partial[blockIdx.x].
+// MODE 2: fused defect pass of the mixed solver -- x += scale*e (when e is
+//         given), w_L = A_L x; interior points get r = f - (w_L + 0.1 x) and
+//         the interior part of r'Cr; boundary points keep w_L.
 template <typename T>
 struct AxArgs {
   T *w;
   const T *u;        // MODE 0 input; MODE 1: z
-  T *p;              // MODE 1: search direction (read old, write new)
+  T *p;              // MODE 1: search direction (read old, write new); MODE 2: x
   const T *g;        // gxyz(6, nxyz, nelt)
-  const T *c;        // MODE 1: inverse multiplicity
+  const T *c;        // MODE 1/2: inverse multiplicity
   const T *D;        // dxm1(lx1,lx1) column-major: D(i,m) at D[i + m*lx1]
   const CgScalars *sc;
   double *partial;
   int first;         // MODE 1: first iteration (beta = 0)
   int nelt;
+  const T *f;        // MODE 2: right-hand side
+  T *r;              // MODE 2: residual (interior points)
+  const float *e;    // MODE 2: FP32 correction added to x first (may be null)
+  double scale;      // MODE 2: its scale
 };
 
 template <typename T, int LX>
 struct AxShared {
-  T u[LX * LX * LX];
-  T wr[LX * LX * LX];
-  T ws[LX * LX * LX];
-  T Dp[LX * (LX + 1)];   // Dp[i*(LX+1)+m] = D(i,m)
-  T Dtp[LX * (LX + 1)];  // Dtp[i*(LX+1)+m] = D(m,i)
+  alignas(16) T u[LX * LX * LX];
+  alignas(16) T wr[LX * LX * LX];
+  alignas(16) T ws[LX * LX * LX];
+  T Dp[LX * (LX + 1)];   // Dp[i*(LX+1)+m] = D(i,m)   (FP64 kernel)
+  T Dtp[LX * (LX + 1)];  // Dtp[i*(LX+1)+m] = D(m,i)  (FP64 kernel)
+  alignas(16) T Dr[LX * LX];  // Dr[k*LX+m] = D(k,m)   (register-D kernel)
+  alignas(16) T Dc[LX * LX];  // Dc[k*LX+m] = D(m,k)
   double red[32];
 };
 
-template <typename T, int LX, int MODE>
+// Sum over m of coef[m] * data[m] in the reference's order (first product,
+// then fused multiply-adds); data contiguous in shared memory and read with
+// the widest aligned vector loads.
+template <typename T, int LX>
+__device__ __forceinline__ T dot_contig(const T *coef, const T *data) {
+  T v[LX];
+  if (sizeof(T) == 4 && LX % 4 == 0) {
+#pragma unroll
+    for (int q = 0; q < LX / 4; ++q) {
+      const float4 t = reinterpret_cast<const float4 *>(data)[q];
+      v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+    }
+  } else if (sizeof(T) == 4 && LX % 2 == 0) {
+#pragma unroll
+    for (int q = 0; q < LX / 2; ++q) {
+      const float2 t = reinterpret_cast<const float2 *>(data)[q];
+      v[2 * q] = t.x; v[2 * q + 1] = t.y;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < LX; ++q) v[q] = data[q];
+  }
+  T s = mul_rn(coef[0], v[0]);
+#pragma unroll
+  for (int m = 1; m < LX; ++m) s = fma_rn(coef[m], v[m], s);
+  return s;
+}
+
+// Element operator.  RD (register D): the thread keeps D(i,:), D(j,:),
+// D(:,i), D(:,j) in registers and reads rows of the element and of D with
+// vector loads -- the FP32 variant, where shared-memory bandwidth, not
+// arithmetic, limits; the FP64 variant reads D from padded shared memory
+// (the FP64 pipe limits there, and registers go to occupancy).
+template <typename T, int LX, int MODE, bool RD>
 __global__ void __launch_bounds__(LX * LX)
-    k_ax(AxArgs<T> a) {
+    k_ax_impl(AxArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   AxShared<T, LX> &sm = *reinterpret_cast<AxShared<T, LX> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, LP = LX + 1;
@@ -123,11 +165,16 @@ __global__ void __launch_bounds__(LX * LX)
   const int e = blockIdx.x;
   const size_t base = size_t(e) * L3;
 
-  for (int q = tid; q < L2; q += L2) {
-    const int r = q % LX, m = q / LX;  // D(r,m)
+  {
+    const int r = tid % LX, m = tid / LX;  // D(r,m)
     const T d = a.D[r + m * LX];
-    sm.Dp[r * LP + m] = d;
-    sm.Dtp[m * LP + r] = d;
+    if (RD) {
+      sm.Dr[r * LX + m] = d;
+      sm.Dc[m * LX + r] = d;
+    } else {
+      sm.Dp[r * LP + m] = d;
+      sm.Dtp[m * LP + r] = d;
+    }
   }
 
   T ureg[LX];
@@ -141,6 +188,12 @@ __global__ void __launch_bounds__(LX * LX)
       const T z = a.u[id];
       v = a.first ? z : fma_rn(beta, a.p[id], z);  // add2s1, math.f:534
       a.p[id] = v;
+    } else if (MODE == 2) {
+      v = a.p[id];
+      if (a.e) {
+        v = fma_rn(T(a.scale), T(a.e[id]), v);
+        a.p[id] = v;
+      }
     } else {
       v = a.u[id];
     }
@@ -149,21 +202,39 @@ __global__ void __launch_bounds__(LX * LX)
   }
   __syncthreads();
 
+  T Di[RD ? LX : 1], Dj[RD ? LX : 1];
+  if (RD) {
+#pragma unroll
+    for (int m = 0; m < LX; ++m) {
+      Di[m] = sm.Dr[i * LX + m];
+      Dj[m] = sm.Dr[j * LX + m];
+    }
+  }
+
   T wtreg[LX];
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     // local_grad3, cg.f:170-187
+    T ur, us, ut;
     const T *urow = &sm.u[k * L2 + j * LX];
-    T ur = mul_rn(sm.Dp[i * LP + 0], urow[0]);
-#pragma unroll
-    for (int m = 1; m < LX; ++m) ur = fma_rn(sm.Dp[i * LP + m], urow[m], ur);
     const T *ucol = &sm.u[k * L2 + i];
-    T us = mul_rn(ucol[0], sm.Dp[j * LP + 0]);
+    if (RD) {
+      ur = dot_contig<T, LX>(Di, urow);
+      us = mul_rn(ucol[0], Dj[0]);
 #pragma unroll
-    for (int m = 1; m < LX; ++m) us = fma_rn(ucol[m * LX], sm.Dp[j * LP + m], us);
-    T ut = mul_rn(ureg[0], sm.Dp[k * LP + 0]);
+      for (int m = 1; m < LX; ++m) us = fma_rn(ucol[m * LX], Dj[m], us);
+      ut = dot_contig<T, LX>(ureg, &sm.Dr[k * LX]);
+    } else {
+      ur = mul_rn(sm.Dp[i * LP + 0], urow[0]);
 #pragma unroll
-    for (int m = 1; m < LX; ++m) ut = fma_rn(ureg[m], sm.Dp[k * LP + m], ut);
+      for (int m = 1; m < LX; ++m) ur = fma_rn(sm.Dp[i * LP + m], urow[m], ur);
+      us = mul_rn(ucol[0], sm.Dp[j * LP + 0]);
+#pragma unroll
+      for (int m = 1; m < LX; ++m) us = fma_rn(ucol[m * LX], sm.Dp[j * LP + m], us);
+      ut = mul_rn(ureg[0], sm.Dp[k * LP + 0]);
+#pragma unroll
+      for (int m = 1; m < LX; ++m) ut = fma_rn(ureg[m], sm.Dp[k * LP + m], ut);
+    }
     // metric, cg.f:156-163
     const size_t pt = base + size_t(k) * L2 + tid;
     typedef typename Vec2<T>::type V2;
@@ -184,34 +255,61 @@ __global__ void __launch_bounds__(LX * LX)
   }
   __syncthreads();
 
+  if (RD) {
+#pragma unroll
+    for (int m = 0; m < LX; ++m) {
+      Di[m] = sm.Dc[i * LX + m];  // D(m,i)
+      Dj[m] = sm.Dc[j * LX + m];  // D(m,j)
+    }
+  }
+
   T part = T(0);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     // local_grad3_t, cg.f:189-212: u = Dt*ur; w = us*D; u += w; w = ut*D; u += w
+    T tr, ts, tt;
     const T *rrow = &sm.wr[k * L2 + j * LX];
-    T tr = mul_rn(sm.Dtp[i * LP + 0], rrow[0]);
-#pragma unroll
-    for (int m = 1; m < LX; ++m) tr = fma_rn(sm.Dtp[i * LP + m], rrow[m], tr);
     const T *scol = &sm.ws[k * L2 + i];
-    T ts = mul_rn(scol[0], sm.Dtp[j * LP + 0]);
+    if (RD) {
+      tr = dot_contig<T, LX>(Di, rrow);
+      ts = mul_rn(scol[0], Dj[0]);
 #pragma unroll
-    for (int m = 1; m < LX; ++m) ts = fma_rn(scol[m * LX], sm.Dtp[j * LP + m], ts);
-    T tt = mul_rn(wtreg[0], sm.Dtp[k * LP + 0]);
+      for (int m = 1; m < LX; ++m) ts = fma_rn(scol[m * LX], Dj[m], ts);
+      tt = dot_contig<T, LX>(wtreg, &sm.Dc[k * LX]);
+    } else {
+      tr = mul_rn(sm.Dtp[i * LP + 0], rrow[0]);
 #pragma unroll
-    for (int m = 1; m < LX; ++m) tt = fma_rn(wtreg[m], sm.Dtp[k * LP + m], tt);
+      for (int m = 1; m < LX; ++m) tr = fma_rn(sm.Dtp[i * LP + m], rrow[m], tr);
+      ts = mul_rn(scol[0], sm.Dtp[j * LP + 0]);
+#pragma unroll
+      for (int m = 1; m < LX; ++m) ts = fma_rn(scol[m * LX], sm.Dtp[j * LP + m], ts);
+      tt = mul_rn(wtreg[0], sm.Dtp[k * LP + 0]);
+#pragma unroll
+      for (int m = 1; m < LX; ++m) tt = fma_rn(wtreg[m], sm.Dtp[k * LP + m], tt);
+    }
     T wl = add_rn(add_rn(tr, ts), tt);
     const size_t id = base + size_t(k) * L2 + tid;
+    const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
+                          (k > 0) && (k < LX - 1);
     if (MODE == 1) {
-      const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
-                            (k > 0) && (k < LX - 1);
       if (interior) {
         wl = fma_rn(T(0.1), ureg[k], wl);  // add2s2(w,u,.1,n), cg.f:119
         part = fma_rn(mul_rn(wl, a.c[id]), ureg[k], part);
       }
+      a.w[id] = wl;
+    } else if (MODE == 2) {
+      if (interior) {
+        const T rv = a.f[id] - fma_rn(T(0.1), ureg[k], wl);
+        a.r[id] = rv;
+        part = fma_rn(mul_rn(rv, a.c[id]), rv, part);
+      } else {
+        a.w[id] = wl;
+      }
+    } else {
+      a.w[id] = wl;
     }
-    a.w[id] = wl;
   }
-  if (MODE == 1) {
+  if (MODE != 0) {
     const double s = block_sum<T>(part, sm.red);
     if (i == 0 && j == 0) a.partial[e] = s;
   }
@@ -263,6 +361,47 @@ __global__ void __launch_bounds__(256)
       const double pap = s1 + s2;
       sc->pap = pap;
       sc->alpha = sc->rtz1 / pap;
+    }
+  }
+}
+
+// ------------------------------------------------- defect boundary pass --
+// Boundary half of MODE 2: t = jl-order group sum of w_L; A x = t + 0.1 x
+// (0 when masked); r = f - A x; r'Cr reduced with the interior partials into
+// sc->rtr and sc->rnorm.
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_gs_res(const T *__restrict__ w, const T *__restrict__ x,
+             const T *__restrict__ f, T *__restrict__ r, const T *__restrict__ c,
+             const int *__restrict__ off, const unsigned *__restrict__ idx, int ng,
+             double *__restrict__ partial, const double *__restrict__ ax_partial,
+             int n_ax_partial, unsigned *counter, CgScalars *sc) {
+  __shared__ double red[32];
+  T part = T(0);
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng;
+       g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    T t = w[idx[b] & 0x7fffffffu];
+    for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
+    for (int q = b; q < e; ++q) {
+      const unsigned m = idx[q];
+      const unsigned id = m & 0x7fffffffu;
+      T ax = fma_rn(T(0.1), x[id], t);
+      if (m & 0x80000000u) ax = T(0);
+      const T rv = f[id] - ax;
+      r[id] = rv;
+      part = fma_rn(mul_rn(rv, c[id]), rv, part);
+    }
+  }
+  const double s = block_sum<T>(part, red);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (last_block(counter, gridDim.x)) {
+    const double s1 = block_sum_array(ax_partial, n_ax_partial, red);
+    __syncthreads();
+    const double s2 = block_sum_array(partial, gridDim.x, red);
+    if (threadIdx.x == 0) {
+      sc->rtr = s1 + s2;
+      sc->rnorm = sqrt(s1 + s2);
     }
   }
 }

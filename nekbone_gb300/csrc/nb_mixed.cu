@@ -228,23 +228,33 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   if (!st && cudaMemsetAsync(x, 0, n * 8, s) != cudaSuccess) st = fail(NB_ERR_CUDA, "memset");
   if (!st) st = vec_copy<double>(r, f, n, s);
   if (!st) st = vec_mask<double>(r, op.d_mask_list, op.n_mask, s);
+  const bool fused = op.fused_ok;
+  if (!st) st = vec_glsc3<double>(r, c, r, n, wk, wk.dot_out + 3, nullptr, 0, 0, s);
+  const double *rr_dev = wk.dot_out + 3;
   while (!st) {
-    if (!st) st = vec_glsc3<double>(r, c, r, n, wk, wk.dot_out + 3, nullptr, 0, 0, s);
     double rr = 0.0;
-    if (!st && cudaMemcpyAsync(&rr, wk.dot_out + 3, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-      st = fail(NB_ERR_CUDA, "copy");
-    if (!st && cudaStreamSynchronize(s) != cudaSuccess) st = fail(NB_ERR_CUDA, "sync");
-    if (st) break;
+    if (cudaMemcpyAsync(&rr, rr_dev, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      st = fail(NB_ERR_CUDA, "nb_cg_mixed: reading the residual norm");
+      break;
+    }
     rn = std::sqrt(rr);
     if (k == 0) rn0 = rn;
     if (rn0 == 0.0 || rn / rn0 <= tol || k >= max_outer) break;
     // inner FP32 solve of A e = r / |r|
     st = dev_scale_to_f32(r32, r, 1.0 / rn, n, s);
     if (!st) st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s);
-    if (!st) st = dev_axpy_f32(x, e32, rn, n, s);
-    // FP64 defect: r = f - A x
-    if (!st) st = apply_ax<double>(op, w, x, g, s);
-    if (!st) st = dev_residual(op, r, f, w, n, s);
+    // FP64 defect: x += |r| e; r = f - A x; r'Cr
+    if (!st && fused) {
+      st = residual_fused(op, wk, x, e32, rn, f, g, c, r, w, s);
+      rr_dev = &wk.sc->rtr;
+    } else if (!st) {
+      st = dev_axpy_f32(x, e32, rn, n, s);
+      if (!st) st = apply_ax<double>(op, w, x, g, s);
+      if (!st) st = dev_residual(op, r, f, w, n, s);
+      if (!st) st = vec_glsc3<double>(r, c, r, n, wk, wk.dot_out + 3, nullptr, 0, 0, s);
+      rr_dev = wk.dot_out + 3;
+    }
     inner += inner_iters;
     ++k;
   }

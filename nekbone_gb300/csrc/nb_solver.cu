@@ -365,42 +365,8 @@ template int vec_glsc3<double>(const double *, const double *, const double *, l
 template int vec_glsc3<float>(const float *, const float *, const float *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t);
 
 // ------------------------------------------------------------ ax launch --
-namespace {
-template <typename T, int LX, int MODE>
-int launch_ax_lx(AxArgs<T> a, cudaStream_t s) {
-  const size_t sm = ax_smem_bytes<T, LX>();
-  static bool attr_set = false;
-  if (!attr_set) {
-    NB_CUDA(cudaFuncSetAttribute(k_ax<T, LX, MODE>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
-    attr_set = true;
-  }
-  k_ax<T, LX, MODE><<<a.nelt, dim3(LX, LX), sm, s>>>(a);
-  NB_CUDA(cudaGetLastError());
-  return NB_OK;
-}
-template <typename T, int MODE>
-int launch_ax_mode(int lx, AxArgs<T> a, cudaStream_t s) {
-  switch (lx) {
-#define NB_CASE(L) case L: return launch_ax_lx<T, L, MODE>(a, s);
-    NB_CASE(2) NB_CASE(3) NB_CASE(4) NB_CASE(5) NB_CASE(6) NB_CASE(7)
-    NB_CASE(8) NB_CASE(9) NB_CASE(10) NB_CASE(11) NB_CASE(12) NB_CASE(13)
-    NB_CASE(14) NB_CASE(15) NB_CASE(16)
-#undef NB_CASE
-    default:
-      return fail(NB_ERR_UNSUPPORTED, "ax: lx1=%d not supported (2..%d)", lx, kMaxLx);
-  }
-}
-}  // namespace
-
-template <typename T>
-int launch_ax(const Operator &op, int mode, AxArgs<T> a, cudaStream_t s) {
-  a.nelt = op.nelt;
-  if (mode == 0) return launch_ax_mode<T, 0>(op.lx, a, s);
-  return launch_ax_mode<T, 1>(op.lx, a, s);
-}
-template int launch_ax<double>(const Operator &, int, AxArgs<double>, cudaStream_t);
-template int launch_ax<float>(const Operator &, int, AxArgs<float>, cudaStream_t);
+// launch_ax<T> is instantiated in nb_ax_f64.cu / nb_ax_f32.cu (one
+// translation unit per precision and mode, so the builds run in parallel).
 
 // maskit (cg.f:214-258) on a device vector: the build branch (zero every
 // element's domain faces, then record element 1's zero entries) on the first
@@ -506,6 +472,79 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
   }
   return NB_OK;
 }
+
+// x += scale*e; r = f - A x; rtr -> sc (MODE 2 + k_gs_res)
+int residual_fused(Operator &op, CgWork &wk, double *x, const float *e,
+                   double scale, const double *f, const double *g,
+                   const double *c, double *r, double *w, cudaStream_t s) {
+  NB_TRY(wk.ensure(op, 1));
+  AxArgs<double> a{};
+  a.w = w;
+  a.p = x;
+  a.g = g;
+  a.c = c;
+  a.D = op.dD;
+  a.sc = wk.sc;
+  a.partial = wk.partial_ax;
+  a.f = f;
+  a.r = r;
+  a.e = e;
+  a.scale = scale;
+  NB_TRY(launch_ax<double>(op, 2, a, s));
+  k_gs_res<double><<<wk.grid_gs, 256, 0, s>>>(w, x, f, r, c, op.bnd_off, op.bnd_idx,
+                                              op.nbg, wk.partial_gs, wk.partial_ax,
+                                              op.nelt, wk.counters + 0, wk.sc);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
+template <typename T>
+int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
+                      const T *c, T *r, T *w, T *p, int reps, double *ms3,
+                      cudaStream_t s) {
+  NB_TRY(cg_begin_t<T>(op, wk, x, f, c, r, true, reps + 2, s));
+  NB_TRY(cg_steps_t<T>(op, wk, x, g, c, r, w, p, r, 1, 1, -1, nullptr, false, s));
+  cudaEvent_t ev[4];
+  for (auto &e : ev) NB_CUDA(cudaEventCreate(&e));
+  double acc[3] = {0, 0, 0};
+  const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
+  for (int it = 0; it < reps; ++it) {
+    AxArgs<T> a{};
+    a.w = w;
+    a.u = r;
+    a.p = p;
+    a.g = g;
+    a.c = c;
+    a.D = D;
+    a.sc = wk.sc;
+    a.partial = wk.partial_ax;
+    NB_CUDA(cudaEventRecord(ev[0], s));
+    NB_TRY(launch_ax<T>(op, 1, a, s));
+    NB_CUDA(cudaEventRecord(ev[1], s));
+    k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx, op.nbg,
+                                           wk.partial_gs, wk.partial_ax, op.nelt,
+                                           wk.counters + 0, wk.sc);
+    NB_CUDA(cudaEventRecord(ev[2], s));
+    k_cg_update<T><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, op.n, wk.partial_up,
+                                              wk.counters + 1, wk.sc, nullptr, it + 2, 1);
+    NB_CUDA(cudaEventRecord(ev[3], s));
+    NB_CUDA(cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+      float ms = 0;
+      NB_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+      acc[k] += ms;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (int k = 0; k < 3; ++k) ms3[k] = acc[k] / (reps > 0 ? reps : 1);
+  return NB_OK;
+}
+template int time_cg_kernels_t<double>(Operator &, CgWork &, double *, const double *,
+                                       const double *, const double *, double *, double *,
+                                       double *, int, double *, cudaStream_t);
+template int time_cg_kernels_t<float>(Operator &, CgWork &, float *, const float *,
+                                      const float *, const float *, float *, float *,
+                                      float *, int, double *, cudaStream_t);
 
 int launch_gs_fin(const Operator &op, CgWork &wk, double *w, const double *p,
                   const double *c, cudaStream_t s) {

@@ -71,6 +71,10 @@ std::vector<int> full_mask_list(const Operator &op);
 // ------------------------------------------------------------- kernels --
 template <typename T>
 int launch_ax(const Operator &op, int mode, AxArgs<T> a, cudaStream_t s);
+template <>
+int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s);
+template <>
+int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s);
 template <typename T>
 int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
               double *out, CgScalars *sc, int mode, int iter, cudaStream_t s);
@@ -107,6 +111,16 @@ int cg_begin(Operator &op, CgWork &wk, double *x, const double *f,
 int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
              const double *c, double *r, double *w, double *p, int it0,
              int it1, cudaStream_t s);
+// mixed solver's fused defect pass: x += scale*e (e may be null);
+// r = f - A x; r'Cr into wk.sc->rtr (fused path only)
+int residual_fused(Operator &op, CgWork &wk, double *x, const float *e,
+                   double scale, const double *f, const double *g,
+                   const double *c, double *r, double *w, cudaStream_t s);
+// CUDA-event times of the three kernels of a fused CG iteration
+template <typename T>
+int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
+                      const T *c, T *r, T *w, T *p, int reps, double *ms3,
+                      cudaStream_t s);
 // the second and third kernels of a fused FP64 iteration, for timing
 int launch_gs_fin(const Operator &op, CgWork &wk, double *w, const double *p,
                   const double *c, cudaStream_t s);
