@@ -576,7 +576,7 @@ void cg_(double *x, const double *f, const double *g, const double *c,
       d2h(p, dp, nn * 8))
     return;
   if (*niter > 0 && d2h(z, dz, nn * 8)) return;
-  if (sync()) return;
+  if (sync() || device_error_check(S.s)) return;
   const int iter = *niter + 1;
   for (int k = 0; k < *niter; ++k) S.flop_a += ax_flops(S.nx1, S.nelt);
   const double inc = double(wrap_mul(wrap_mul(iter, 15), *n));
@@ -819,7 +819,8 @@ int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
 int nb_sync(void) {
   clear_status();
   if (st().init()) return last_status();
-  return sync();
+  NB_TRY(sync());
+  return device_error_check(st().s);
 }
 
 }  // extern "C"

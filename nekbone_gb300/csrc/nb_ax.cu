@@ -13,6 +13,7 @@ int launch_ax_f32_m2(int lx, AxArgs<float> a, cudaStream_t s);
 template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
   a.nelt = op.nelt;
+  a.err = device_error_word();
   if (mode == 0) return launch_ax_f64_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f64_m1(op.lx, a, s);
   return launch_ax_f64_m2(op.lx, a, s);
@@ -21,6 +22,7 @@ int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream
 template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
   a.nelt = op.nelt;
+  a.err = device_error_word();
   if (mode == 0) return launch_ax_f32_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f32_m1(op.lx, a, s);
   return launch_ax_f32_m2(op.lx, a, s);

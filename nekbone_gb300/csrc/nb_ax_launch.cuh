@@ -7,9 +7,30 @@
 
 namespace nb {
 
+// FP32, even lx1, modes 0/1, metric pointer 16-byte aligned: the bulk-copy
+// kernel; otherwise the general one.
+template <int LX, int MODE>
+int launch_ax_f32_tma(AxArgs<float> a, cudaStream_t s) {
+  const size_t sm = ax_tma_smem_bytes<LX>();
+  static bool attr_set = false;
+  if (!attr_set) {
+    NB_CUDA(cudaFuncSetAttribute(k_ax_f32_tma<LX, MODE>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    attr_set = true;
+  }
+  k_ax_f32_tma<LX, MODE><<<a.nelt, dim3(LX, LX), sm, s>>>(a);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
 template <typename T, int LX, int MODE>
 int launch_ax_lx(AxArgs<T> a, cudaStream_t s) {
   constexpr bool RD = std::is_same<T, float>::value;
+  if constexpr (std::is_same<T, float>::value && LX % 2 == 0 && MODE != 2 &&
+                sizeof(AxTmaShared<LX>) <= 227 * 1024) {
+    if ((reinterpret_cast<uintptr_t>(a.g) & 15u) == 0)
+      return launch_ax_f32_tma<LX, MODE>(reinterpret_cast<AxArgs<float> &>(a), s);
+  }
   const size_t sm = ax_smem_bytes<T, LX>();
   static bool attr_set = false;
   if (!attr_set) {

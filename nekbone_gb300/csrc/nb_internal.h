@@ -53,6 +53,11 @@ void set_error_mode(int mode);
     if (s_ != 0) return s_;     \
   } while (0)
 
+// The device error word of bounded waits (allocated on first use) and its
+// check, which synchronises the stream and fails if a wait ran out.
+unsigned *device_error_word();
+int device_error_check(cudaStream_t s);
+
 constexpr int kMaxLx = 16;     // largest lx1 with a specialised ax kernel
 constexpr int kMaxNl = 24;     // largest 1-D size of a multigrid tensor apply
 

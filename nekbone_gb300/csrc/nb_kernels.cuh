@@ -107,6 +107,7 @@ struct AxArgs {
   T *r;              // MODE 2: residual (interior points)
   const float *e;    // MODE 2: FP32 correction added to x first (may be null)
   double scale;      // MODE 2: its scale
+  unsigned *err;     // device error word for bounded waits (may be null)
 };
 
 template <typename T, int LX>
@@ -157,7 +158,7 @@ __device__ __forceinline__ T dot_contig(const T *coef, const T *data) {
 template <typename T, int LX, int MODE, bool RD>
 __global__ void __launch_bounds__(LX * LX)
     k_ax_impl(AxArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   AxShared<T, LX> &sm = *reinterpret_cast<AxShared<T, LX> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, LP = LX + 1;
   const int i = threadIdx.x, j = threadIdx.y;
@@ -491,6 +492,144 @@ __global__ void __launch_bounds__(256)
       }
     }
   }
+}
+
+}  // namespace nb
+
+#include "nb_tma.cuh"
+
+namespace nb {
+
+// ------------------------------------------- FP32 operator, TMA metric --
+// The FP32 element operator with the element's whole metric block
+// (24*lx1^3 bytes, contiguous in gxyz(6,nxyz,nelt)) brought into shared
+// memory by one bulk copy issued when the CTA starts.  The copy overlaps the
+// loads of z and the old p; the arithmetic is that of k_ax_impl<float,..,RD>
+// (same order, same results).  Even lx1 only (the copy size must be a
+// multiple of 16 bytes).
+template <int LX>
+struct AxTmaShared {
+  alignas(128) float g[6 * LX * LX * LX];
+  alignas(16) float u[LX * LX * LX];
+  alignas(16) float wr[LX * LX * LX];
+  alignas(16) float ws[LX * LX * LX];
+  alignas(16) float Dr[LX * LX];
+  alignas(16) float Dc[LX * LX];
+  alignas(8) uint64_t bar;
+  double red[32];
+};
+
+template <int LX, int MODE>
+__global__ void __launch_bounds__(LX * LX)
+    k_ax_f32_tma(AxArgs<float> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  AxTmaShared<LX> &sm = *reinterpret_cast<AxTmaShared<LX> *>(smem_raw);
+  constexpr int L2 = LX * LX, L3 = LX * LX * LX;
+  constexpr unsigned GBYTES = 24u * L3;
+  const int i = threadIdx.x, j = threadIdx.y;
+  const int tid = i + LX * j;
+  const int e = blockIdx.x;
+  const size_t base = size_t(e) * L3;
+
+  if (tid == 0) {
+    mbar_init(&sm.bar, 1);
+    mbar_arrive_expect_tx(&sm.bar, GBYTES);
+    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
+  }
+  {
+    const int r = tid % LX, m = tid / LX;
+    const float d = a.D[r + m * LX];
+    sm.Dr[r * LX + m] = d;
+    sm.Dc[m * LX + r] = d;
+  }
+  float ureg[LX];
+  float beta = 0.f;
+  if (MODE == 1 && !a.first) beta = float(a.sc->beta);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + tid;
+    float v;
+    if (MODE == 1) {
+      const float z = a.u[id];
+      v = a.first ? z : fma_rn(beta, a.p[id], z);
+      a.p[id] = v;
+    } else {
+      v = a.u[id];
+    }
+    ureg[k] = v;
+    sm.u[k * L2 + tid] = v;
+  }
+  __syncthreads();
+  float Di[LX], Dj[LX];
+#pragma unroll
+  for (int m = 0; m < LX; ++m) {
+    Di[m] = sm.Dr[i * LX + m];
+    Dj[m] = sm.Dr[j * LX + m];
+  }
+  mbar_wait_bounded(&sm.bar, 0, a.err);
+
+  float wtreg[LX];
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const float *urow = &sm.u[k * L2 + j * LX];
+    const float *ucol = &sm.u[k * L2 + i];
+    const float ur = dot_contig<float, LX>(Di, urow);
+    float us = mul_rn(ucol[0], Dj[0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) us = fma_rn(ucol[m * LX], Dj[m], us);
+    const float ut = dot_contig<float, LX>(ureg, &sm.Dr[k * LX]);
+    const float2 *gp = reinterpret_cast<const float2 *>(&sm.g[6 * (k * L2 + tid)]);
+    const float2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
+    float wr = mul_rn(g01.x, ur);
+    wr = fma_rn(g01.y, us, wr);
+    wr = fma_rn(g23.x, ut, wr);
+    float ws = mul_rn(g01.y, ur);
+    ws = fma_rn(g23.y, us, ws);
+    ws = fma_rn(g45.x, ut, ws);
+    float wt = mul_rn(g23.x, ur);
+    wt = fma_rn(g45.x, us, wt);
+    wt = fma_rn(g45.y, ut, wt);
+    sm.wr[k * L2 + tid] = wr;
+    sm.ws[k * L2 + tid] = ws;
+    wtreg[k] = wt;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int m = 0; m < LX; ++m) {
+    Di[m] = sm.Dc[i * LX + m];
+    Dj[m] = sm.Dc[j * LX + m];
+  }
+  float part = 0.f;
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const float *rrow = &sm.wr[k * L2 + j * LX];
+    const float *scol = &sm.ws[k * L2 + i];
+    const float tr = dot_contig<float, LX>(Di, rrow);
+    float ts = mul_rn(scol[0], Dj[0]);
+#pragma unroll
+    for (int m = 1; m < LX; ++m) ts = fma_rn(scol[m * LX], Dj[m], ts);
+    const float tt = dot_contig<float, LX>(wtreg, &sm.Dc[k * LX]);
+    float wl = add_rn(add_rn(tr, ts), tt);
+    const size_t id = base + size_t(k) * L2 + tid;
+    if (MODE == 1) {
+      const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
+                            (k > 0) && (k < LX - 1);
+      if (interior) {
+        wl = fma_rn(0.1f, ureg[k], wl);
+        part = fma_rn(mul_rn(wl, a.c[id]), ureg[k], part);
+      }
+    }
+    a.w[id] = wl;
+  }
+  if (MODE == 1) {
+    const double s = block_sum<float>(part, sm.red);
+    if (i == 0 && j == 0) a.partial[e] = s;
+  }
+}
+
+template <int LX>
+constexpr size_t ax_tma_smem_bytes() {
+  return sizeof(AxTmaShared<LX>);
 }
 
 }  // namespace nb
