@@ -56,6 +56,12 @@ void nekbone_set_mask_mode_(const int *mode);
 /* .true. selects h1mg_solve as solveM (MGRID build, cg.f:86-94,
  * hsmg.f:960); .false. the copy of hsmg_dum.f:9-14. */
 void nekbone_set_mgrid_(const int *ifmgrid);
+/* Summation order of the FP64 element contractions: 0 = the reference's
+ * left-to-right mxm sums (mxm_std.f:255; bit-identical to a left-to-right
+ * fma evaluation), 1 = even-odd split of the anti-centrosymmetric GLL
+ * derivative (default; same result to rounding, ~27% fewer FP64 operations).
+ * ax_e_ always uses order 0. */
+void nekbone_set_contraction_order_(const int *order);
 /* /cflops/ flop_a, flop_cg (INPUT:8), accumulated as the reference does */
 void nekbone_get_flops_(double *flop_a, double *flop_cg);
 void nekbone_set_flops_(const double *flop_a, const double *flop_cg);
@@ -142,6 +148,9 @@ typedef struct nb_mesh nb_mesh;
 int  nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
                     int mask_mode);
 int  nb_mesh_destroy(nb_mesh *mesh);
+/* contraction order of this mesh's FP64 operator (see
+ * nekbone_set_contraction_order_) */
+int  nb_mesh_set_order(nb_mesh *mesh, int order);
 long nb_mesh_npts(const nb_mesh *mesh);
 int  nb_mesh_info(const nb_mesh *mesh, int *nelt, int *lx1, int *fused);
 

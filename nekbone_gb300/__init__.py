@@ -39,7 +39,8 @@ EXPORTS = (
     "nekbone_last_status", "nekbone_last_message", "nekbone_clear_status",
     "nekbone_set_error_mode", "nekbone_version", "nekbone_common_",
     "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
-    "nekbone_get_flops_", "nekbone_set_flops_", "gs_setup_", "gs_op_",
+    "nekbone_get_flops_", "nekbone_set_flops_", "nekbone_set_contraction_order_",
+    "nb_mesh_set_order", "gs_setup_", "gs_op_",
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
@@ -59,6 +60,8 @@ for _name in ("nb_mesh_create", "nb_mesh_destroy", "nb_mesh_info", "nb_setup_g",
               "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync"):
     getattr(lib, _name).restype = _i
 lib.nb_mesh_npts.argtypes = [_p]
+lib.nb_mesh_set_order.restype = _i
+lib.nb_mesh_set_order.argtypes = [_p, _i]
 lib.nb_mesh_destroy.argtypes = [_p]
 lib.nb_rhs_uniform.argtypes = [_p, _p, _p, _C.c_uint64]
 lib.nb_cg.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _p, _i, _i, _p]
@@ -272,6 +275,12 @@ class Nekbone:
     def mask_reset(self) -> None:
         lib.nekbone_mask_reset_()
 
+    @staticmethod
+    def set_order(order: int) -> None:
+        """0 = reference left-to-right contraction sums, 1 = even-odd split."""
+        lib.nekbone_set_contraction_order_(_ref(order))
+        _check()
+
     def set_mgrid(self, on: bool) -> None:
         lib.nekbone_set_mgrid_(_ref(1 if on else 0))
 
@@ -351,6 +360,9 @@ class DeviceMesh:
             self.close()
         except Exception:
             pass
+
+    def set_order(self, order: int) -> None:
+        _check(lib.nb_mesh_set_order(self._h, order))
 
     def setup_g(self, g_ptr: int) -> None:
         _check(lib.nb_setup_g(self._h, _p(g_ptr)))

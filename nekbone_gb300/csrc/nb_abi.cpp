@@ -98,6 +98,7 @@ struct State {
   std::vector<int> lglel;
   std::vector<double> dxm1;
   int mask_mode = 0;
+  int order = 1;  // contraction order of the FP64 operator (1 even-odd)
   bool mgrid = false;
   double flop_a = 0.0, flop_cg = 0.0;
   std::unique_ptr<Operator> op;
@@ -152,6 +153,7 @@ int common_op(Operator **out) {
     std::unique_ptr<Operator> op(new Operator());
     NB_TRY(operator_from(op.get(), S.nelx, S.nely, S.nelz, S.nelt, S.nx1,
                          S.lglel.data(), S.dxm1.data(), g->host, S.mask_mode, S.s));
+    op->order = S.order;
     S.op = std::move(op);
   }
   *out = S.op.get();
@@ -255,6 +257,16 @@ void nekbone_set_mask_mode_(const int *mode) {
 }
 
 void nekbone_set_mgrid_(const int *ifmgrid) { st().mgrid = *ifmgrid != 0; }
+
+void nekbone_set_contraction_order_(const int *order) {
+  clear_status();
+  if (*order != 0 && *order != 1) {
+    fail(NB_ERR_ARG, "contraction order %d not 0 or 1", *order);
+    return;
+  }
+  st().order = *order;
+  if (st().op) st().op->order = *order;
+}
 
 void nekbone_get_flops_(double *flop_a, double *flop_cg) {
   *flop_a = st().flop_a;
@@ -446,7 +458,7 @@ void ax_e_(double *w, const double *u, const double *g, double *ur,
   double *dw, *du, *dg, *dD;
   if (dbuf(0, m3, &dw) || dbuf(1, m3, &du) || dbuf(2, 6 * m3, &dg) || dbuf(3, lx * lx, &dD)) return;
   if (h2d(du, u, m3 * 8) || h2d(dg, g, 6 * m3 * 8) || h2d(dD, S.dxm1.data(), lx * lx * 8)) return;
-  Operator one;
+  Operator one;  // no even-odd tables: the reference's left-to-right sums
   one.lx = lx;
   one.nelt = 1;
   one.n = m3;
@@ -690,6 +702,14 @@ int nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
   std::unique_ptr<nb_mesh> m(new nb_mesh());
   NB_TRY(operator_box(&m->op, nelx, nely, nelz, lx1, mask_mode, st().s));
   *mesh = m.release();
+  return NB_OK;
+}
+
+int nb_mesh_set_order(nb_mesh *mesh, int order) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (order != 0 && order != 1) return fail(NB_ERR_ARG, "order %d not 0 or 1", order);
+  mesh->op.order = order;
   return NB_OK;
 }
 

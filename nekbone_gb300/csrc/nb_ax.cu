@@ -6,6 +6,9 @@ namespace nb {
 int launch_ax_f64_m0(int lx, AxArgs<double> a, cudaStream_t s);
 int launch_ax_f64_m1(int lx, AxArgs<double> a, cudaStream_t s);
 int launch_ax_f64_m2(int lx, AxArgs<double> a, cudaStream_t s);
+int launch_ax_eo_m0(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
+int launch_ax_eo_m1(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
+int launch_ax_eo_m2(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
 int launch_ax_f32_m0(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m1(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m2(int lx, AxArgs<float> a, cudaStream_t s);
@@ -14,6 +17,11 @@ template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
+  if (op.order == 1 && op.eo_ok && op.dEO) {  // even-odd split (FP64 pipe bound)
+    if (mode == 0) return launch_ax_eo_m0(op.lx, a, op.dEO, s);
+    if (mode == 1) return launch_ax_eo_m1(op.lx, a, op.dEO, s);
+    return launch_ax_eo_m2(op.lx, a, op.dEO, s);
+  }
   if (mode == 0) return launch_ax_f64_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f64_m1(op.lx, a, s);
   return launch_ax_f64_m2(op.lx, a, s);

@@ -1,0 +1,8 @@
+// Even-odd FP64 element operator instantiations, mode 1 (nb_kernels.cuh).
+#include "nb_ax_eo_launch.cuh"
+
+namespace nb {
+int launch_ax_eo_m1(int lx, AxArgs<double> a, const double *eo, cudaStream_t s) {
+  return launch_ax_eo_mode<1>(lx, a, eo, s);
+}
+}  // namespace nb

@@ -179,6 +179,18 @@ __global__ void __launch_bounds__(LX * LX)
   }
 
   T ureg[LX];
+  // c (and f) are needed only at interior points; they are fetched with the
+  // element, not inside the epilogue, so that no load waits behind a store
+  const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
+  T creg[LX], freg[LX];
+  if (MODE != 0 && col_interior) {
+#pragma unroll
+    for (int k = 1; k < LX - 1; ++k) {
+      const size_t id = base + size_t(k) * L2 + tid;
+      creg[k] = a.c[id];
+      if (MODE == 2) freg[k] = a.f[id];
+    }
+  }
   T beta = T(0);
   if (MODE == 1 && !a.first) beta = T(a.sc->beta);
 #pragma unroll
@@ -290,19 +302,18 @@ __global__ void __launch_bounds__(LX * LX)
     }
     T wl = add_rn(add_rn(tr, ts), tt);
     const size_t id = base + size_t(k) * L2 + tid;
-    const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
-                          (k > 0) && (k < LX - 1);
+    const bool interior = col_interior && (k > 0) && (k < LX - 1);
     if (MODE == 1) {
       if (interior) {
         wl = fma_rn(T(0.1), ureg[k], wl);  // add2s2(w,u,.1,n), cg.f:119
-        part = fma_rn(mul_rn(wl, a.c[id]), ureg[k], part);
+        part = fma_rn(mul_rn(wl, creg[k]), ureg[k], part);
       }
       a.w[id] = wl;
     } else if (MODE == 2) {
       if (interior) {
-        const T rv = a.f[id] - fma_rn(T(0.1), ureg[k], wl);
+        const T rv = freg[k] - fma_rn(T(0.1), ureg[k], wl);
         a.r[id] = rv;
-        part = fma_rn(mul_rn(rv, a.c[id]), rv, part);
+        part = fma_rn(mul_rn(rv, creg[k]), rv, part);
       } else {
         a.w[id] = wl;
       }
@@ -543,6 +554,12 @@ __global__ void __launch_bounds__(LX * LX)
     sm.Dc[m * LX + r] = d;
   }
   float ureg[LX];
+  const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
+  float creg[LX];
+  if (MODE == 1 && col_interior) {
+#pragma unroll
+    for (int k = 1; k < LX - 1; ++k) creg[k] = a.c[base + size_t(k) * L2 + tid];
+  }
   float beta = 0.f;
   if (MODE == 1 && !a.first) beta = float(a.sc->beta);
 #pragma unroll
@@ -612,11 +629,9 @@ __global__ void __launch_bounds__(LX * LX)
     float wl = add_rn(add_rn(tr, ts), tt);
     const size_t id = base + size_t(k) * L2 + tid;
     if (MODE == 1) {
-      const bool interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1) &&
-                            (k > 0) && (k < LX - 1);
-      if (interior) {
+      if (col_interior && k > 0 && k < LX - 1) {
         wl = fma_rn(0.1f, ureg[k], wl);
-        part = fma_rn(mul_rn(wl, a.c[id]), ureg[k], part);
+        part = fma_rn(mul_rn(wl, creg[k]), ureg[k], part);
       }
     }
     a.w[id] = wl;
@@ -630,6 +645,220 @@ __global__ void __launch_bounds__(LX * LX)
 template <int LX>
 constexpr size_t ax_tma_smem_bytes() {
   return sizeof(AxTmaShared<LX>);
+}
+
+}  // namespace nb
+
+namespace nb {
+
+// ------------------------------------------ FP64 operator, even-odd split --
+// The GLL derivative matrix is anti-centrosymmetric, D(n-1-i,n-1-m) =
+// -D(i,m) (n = lx1, even here), so each 1-D contraction y = D v splits into
+// an even and an odd half (Solomonoff's even-odd decomposition):
+//   ve(m) = v(m) + v(n-1-m),  vo(m) = v(m) - v(n-1-m),          m < n/2
+//   ye(a) = sum_m E(a,m) ve(m), yo(a) = sum_m O(a,m) vo(m),      a < n/2
+//   y(a) = ye(a) + yo(a),   y(n-1-a) = yo(a) - ye(a)
+// with E(a,m) = (D(a,m) + D(a,n-1-m))/2, O(a,m) = (D(a,m) - D(a,n-1-m))/2.
+// Per output that is n/2 fused multiply-adds plus two additions instead of n
+// multiply-adds: the FP64 pipe, which bounds this kernel on GB300, does ~27%
+// less work per point.  Sums are taken in a different order from the
+// reference's left-to-right mxm, so results agree with it to rounding, not
+// bit for bit (the reference-order kernel stays available).
+//
+// One CTA per element, lx1*lx1 threads.  Thread t owns, in turn, the line
+// (j,k)=(t%n,t/n) of the r contraction, the line (i,k) of the s contraction
+// and its own column (i,j) of the t contraction (kept in registers).
+// Shared arrays use a row pitch of n+1 doubles (bank-conflict free lines).
+template <int LX>
+struct AxEoShared {
+  static constexpr int P = LX + 1;
+  static constexpr int N = P * LX * LX;
+  double A[N];
+  double B[N];
+  double C[N];
+  double E4[4 * (LX / 2) * (LX / 2)];  // E, O of D, then E, O of D^T
+  double red[32];
+};
+
+template <int LX>
+__device__ __forceinline__ int eo_at(int i, int j, int k) {
+  return i + (LX + 1) * j + (LX + 1) * LX * k;
+}
+
+// y(0..n-1) of a folded line v (length n), coefficients Ec/Oc (h x h, row a)
+template <int LX>
+__device__ __forceinline__ void eo_line(const double *v, const double *Ec,
+                                        const double *Oc, double *y) {
+  constexpr int H = LX / 2;
+  double ve[H], vo[H];
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    ve[m] = add_rn(v[m], v[LX - 1 - m]);
+    vo[m] = v[m] - v[LX - 1 - m];
+  }
+#pragma unroll
+  for (int a = 0; a < H; ++a) {
+    double ye = mul_rn(Ec[a * H], ve[0]);
+    double yo = mul_rn(Oc[a * H], vo[0]);
+#pragma unroll
+    for (int m = 1; m < H; ++m) {
+      ye = fma_rn(Ec[a * H + m], ve[m], ye);
+      yo = fma_rn(Oc[a * H + m], vo[m], yo);
+    }
+    y[a] = add_rn(ye, yo);
+    y[LX - 1 - a] = yo - ye;
+  }
+}
+
+template <int LX, int MODE>
+__global__ void __launch_bounds__(LX * LX)
+    k_ax_eo(AxArgs<double> a, const double *eo) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  AxEoShared<LX> &sm = *reinterpret_cast<AxEoShared<LX> *>(smem_raw);
+  constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
+  const int t = threadIdx.x + LX * threadIdx.y;
+  const int i = threadIdx.x, j = threadIdx.y;  // own column (i,j)
+  const int e = blockIdx.x;
+  const size_t base = size_t(e) * L3;
+  const double *Ed = sm.E4, *Od = sm.E4 + H * H;            // of D
+  const double *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;  // of D^T
+
+  for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = eo[q];
+
+  const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
+  double creg[LX], freg[LX];
+  if (MODE != 0 && col_interior) {
+#pragma unroll
+    for (int k = 1; k < LX - 1; ++k) {
+      const size_t id = base + size_t(k) * L2 + t;
+      creg[k] = a.c[id];
+      if (MODE == 2) freg[k] = a.f[id];
+    }
+  }
+  double ureg[LX];
+  const double beta = (MODE == 1 && !a.first) ? a.sc->beta : 0.0;
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + t;
+    double v;
+    if (MODE == 1) {
+      const double z = a.u[id];
+      v = a.first ? z : fma_rn(beta, a.p[id], z);  // add2s1, math.f:534
+      a.p[id] = v;
+    } else if (MODE == 2) {
+      v = a.p[id];
+      if (a.e) {
+        v = fma_rn(a.scale, double(a.e[id]), v);
+        a.p[id] = v;
+      }
+    } else {
+      v = a.u[id];
+    }
+    ureg[k] = v;
+    sm.A[eo_at<LX>(i, j, k)] = v;
+  }
+  __syncthreads();
+
+  // gradient (local_grad3, cg.f:170-187) as three folded contractions
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    double v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(m, l0, l1)];  // line (j,k)
+    eo_line<LX>(v, Ed, Od, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(m, l0, l1)] = y[m];  // ur
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(l0, m, l1)];  // line (i,k)
+    eo_line<LX>(v, Ed, Od, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.C[eo_at<LX>(l0, m, l1)] = y[m];  // us
+  }
+  double wtreg[LX];
+  eo_line<LX>(ureg, Ed, Od, wtreg);  // ut of the own column
+  __syncthreads();
+
+  // metric, cg.f:156-163 (wr, ws back into B, C; wt in registers)
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = eo_at<LX>(i, j, k);
+    const double ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
+    const size_t pt = base + size_t(k) * L2 + t;
+    const double2 *gp = reinterpret_cast<const double2 *>(a.g + 6 * pt);
+    const double2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
+    double wr = mul_rn(g01.x, ur);
+    wr = fma_rn(g01.y, us, wr);
+    wr = fma_rn(g23.x, ut, wr);
+    double ws = mul_rn(g01.y, ur);
+    ws = fma_rn(g23.y, us, ws);
+    ws = fma_rn(g45.x, ut, ws);
+    double wt = mul_rn(g23.x, ur);
+    wt = fma_rn(g45.x, us, wt);
+    wt = fma_rn(g45.y, ut, wt);
+    sm.B[q] = wr;
+    sm.C[q] = ws;
+    wtreg[k] = wt;
+  }
+  __syncthreads();
+
+  // transposed gradient (local_grad3_t, cg.f:189-212) with D^T
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    double v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<LX>(m, l0, l1)];  // wr line (j,k)
+    eo_line<LX>(v, Et, Ot, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.A[eo_at<LX>(m, l0, l1)] = y[m];  // tr
+  }
+  __syncthreads();
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    double v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<LX>(l0, m, l1)];  // ws line (i,k)
+    eo_line<LX>(v, Et, Ot, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(l0, m, l1)] = y[m];  // ts
+  }
+  double ttreg[LX];
+  eo_line<LX>(wtreg, Et, Ot, ttreg);
+  __syncthreads();
+
+  double part = 0.0;
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = eo_at<LX>(i, j, k);
+    double wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
+    const size_t id = base + size_t(k) * L2 + t;
+    const bool interior = col_interior && (k > 0) && (k < LX - 1);
+    if (MODE == 1) {
+      if (interior) {
+        wl = fma_rn(0.1, ureg[k], wl);
+        part = fma_rn(mul_rn(wl, creg[k]), ureg[k], part);
+      }
+      a.w[id] = wl;
+    } else if (MODE == 2) {
+      if (interior) {
+        const double rv = freg[k] - fma_rn(0.1, ureg[k], wl);
+        a.r[id] = rv;
+        part = fma_rn(mul_rn(rv, creg[k]), rv, part);
+      } else {
+        a.w[id] = wl;
+      }
+    } else {
+      a.w[id] = wl;
+    }
+  }
+  if (MODE != 0) {
+    const double s = block_sum<double>(part, sm.red);
+    if (t == 0) a.partial[e] = s;
+  }
+}
+
+template <int LX>
+constexpr size_t ax_eo_smem_bytes() {
+  return sizeof(AxEoShared<LX>);
 }
 
 }  // namespace nb

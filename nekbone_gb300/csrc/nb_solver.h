@@ -18,6 +18,11 @@ struct Operator {
   std::vector<double> D;           // dxm1, column-major
   double *dD = nullptr;
   float *fD = nullptr;
+  // even-odd split of D (E, O of D and of D^T, 4*(lx/2)^2); valid when lx is
+  // even and D is anti-centrosymmetric to rounding
+  double *dEO = nullptr;
+  bool eo_ok = false;
+  int order = 1;                   // 0 reference left-to-right sums, 1 even-odd
   GsHost gsh_host;                 // jl maps of the dssum handle
   GsDevice gs;                     // device form
   // mask state (maskit, cg.f:214-258)

@@ -129,9 +129,18 @@ def test_ax_bitexact(nb, dims, mask_mode):
     ctx = O.Ctx(nelx, nely, nelz, nx, mask_mode=mask_mode)
     rng = np.random.default_rng(5)
     g = rng.standard_normal(6 * mesh.n)         # a general (deformed) metric
-    for _ in range(2):                         # first call builds the mask list
+    nb.Nekbone.set_order(0)                     # the reference's summation order
+    try:
+        for _ in range(2):                     # first call builds the mask list
+            u = rng.standard_normal(mesh.n)
+            assert np.array_equal(mesh.ax(u, g), ctx.ax(u, g))
+        # the even-odd order agrees to rounding
+        nb.Nekbone.set_order(1)
         u = rng.standard_normal(mesh.n)
-        assert np.array_equal(mesh.ax(u, g), ctx.ax(u, g))
+        ref = ctx.ax(u, g)
+        assert rel(mesh.ax(u, g), ref) < 1e-13
+    finally:
+        nb.Nekbone.set_order(1)
 
 
 def test_blas1(nb):
