@@ -193,25 +193,34 @@ __global__ void __launch_bounds__(LX * LX)
   }
   T beta = T(0);
   if (MODE == 1 && !a.first) beta = T(a.sc->beta);
+  // every load of the element is issued before the first store (p or x may
+  // alias nothing, but the compiler cannot know: a store between loads would
+  // serialise them)
+  T pold[LX];
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const size_t id = base + size_t(k) * L2 + tid;
-    T v;
     if (MODE == 1) {
-      const T z = a.u[id];
-      v = a.first ? z : fma_rn(beta, a.p[id], z);  // add2s1, math.f:534
-      a.p[id] = v;
+      ureg[k] = a.u[id];
+      pold[k] = a.first ? T(0) : a.p[id];
     } else if (MODE == 2) {
-      v = a.p[id];
-      if (a.e) {
-        v = fma_rn(T(a.scale), T(a.e[id]), v);
-        a.p[id] = v;
-      }
+      ureg[k] = a.p[id];
+      pold[k] = a.e ? T(a.e[id]) : T(0);
     } else {
-      v = a.u[id];
+      ureg[k] = a.u[id];
     }
-    ureg[k] = v;
-    sm.u[k * L2 + tid] = v;
+  }
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + tid;
+    if (MODE == 1) {
+      if (!a.first) ureg[k] = fma_rn(beta, pold[k], ureg[k]);  // add2s1, math.f:534
+      a.p[id] = ureg[k];
+    } else if (MODE == 2 && a.e) {
+      ureg[k] = fma_rn(T(a.scale), pold[k], ureg[k]);
+      a.p[id] = ureg[k];
+    }
+    sm.u[k * L2 + tid] = ureg[k];
   }
   __syncthreads();
 
@@ -353,14 +362,35 @@ __global__ void __launch_bounds__(256)
     const int b = off[g], e = off[g + 1];
     T t = w[idx[b] & 0x7fffffffu];
     for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
-    for (int q = b; q < e; ++q) {
-      const unsigned m = idx[q];
-      const unsigned id = m & 0x7fffffffu;
-      const T pv = p[id];
-      T v = fma_rn(T(0.1), pv, t);
-      if (m & 0x80000000u) v = T(0);
-      w[id] = v;
-      part = fma_rn(mul_rn(v, c[id]), pv, part);
+    if (e - b <= 8) {
+      // load every member's p and c before the first store of w
+      unsigned mm[8];
+      T pv[8], cv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < e - b) {
+          mm[q] = idx[b + q];
+          pv[q] = p[mm[q] & 0x7fffffffu];
+          cv[q] = c[mm[q] & 0x7fffffffu];
+        }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < e - b) {
+          T v = fma_rn(T(0.1), pv[q], t);
+          if (mm[q] & 0x80000000u) v = T(0);
+          w[mm[q] & 0x7fffffffu] = v;
+          part = fma_rn(mul_rn(v, cv[q]), pv[q], part);
+        }
+    } else {
+      for (int q = b; q < e; ++q) {
+        const unsigned m = idx[q];
+        const unsigned id = m & 0x7fffffffu;
+        const T pv = p[id];
+        T v = fma_rn(T(0.1), pv, t);
+        if (m & 0x80000000u) v = T(0);
+        w[id] = v;
+        part = fma_rn(mul_rn(v, c[id]), pv, part);
+      }
     }
   }
   const double s = block_sum<T>(part, red);
@@ -395,14 +425,37 @@ __global__ void __launch_bounds__(256)
     const int b = off[g], e = off[g + 1];
     T t = w[idx[b] & 0x7fffffffu];
     for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
-    for (int q = b; q < e; ++q) {
-      const unsigned m = idx[q];
-      const unsigned id = m & 0x7fffffffu;
-      T ax = fma_rn(T(0.1), x[id], t);
-      if (m & 0x80000000u) ax = T(0);
-      const T rv = f[id] - ax;
-      r[id] = rv;
-      part = fma_rn(mul_rn(rv, c[id]), rv, part);
+    if (e - b <= 8) {
+      unsigned mm[8];
+      T xv[8], fv[8], cv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < e - b) {
+          mm[q] = idx[b + q];
+          const unsigned id = mm[q] & 0x7fffffffu;
+          xv[q] = x[id];
+          fv[q] = f[id];
+          cv[q] = c[id];
+        }
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < e - b) {
+          T ax = fma_rn(T(0.1), xv[q], t);
+          if (mm[q] & 0x80000000u) ax = T(0);
+          const T rv = fv[q] - ax;
+          r[mm[q] & 0x7fffffffu] = rv;
+          part = fma_rn(mul_rn(rv, cv[q]), rv, part);
+        }
+    } else {
+      for (int q = b; q < e; ++q) {
+        const unsigned m = idx[q];
+        const unsigned id = m & 0x7fffffffu;
+        T ax = fma_rn(T(0.1), x[id], t);
+        if (m & 0x80000000u) ax = T(0);
+        const T rv = f[id] - ax;
+        r[id] = rv;
+        part = fma_rn(mul_rn(rv, c[id]), rv, part);
+      }
     }
   }
   const double s = block_sum<T>(part, red);
@@ -562,19 +615,21 @@ __global__ void __launch_bounds__(LX * LX)
   }
   float beta = 0.f;
   if (MODE == 1 && !a.first) beta = float(a.sc->beta);
+  float pold[LX];
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {  // all loads before the first store
+    const size_t id = base + size_t(k) * L2 + tid;
+    ureg[k] = a.u[id];
+    pold[k] = (MODE == 1 && !a.first) ? a.p[id] : 0.f;
+  }
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const size_t id = base + size_t(k) * L2 + tid;
-    float v;
     if (MODE == 1) {
-      const float z = a.u[id];
-      v = a.first ? z : fma_rn(beta, a.p[id], z);
-      a.p[id] = v;
-    } else {
-      v = a.u[id];
+      if (!a.first) ureg[k] = fma_rn(beta, pold[k], ureg[k]);
+      a.p[id] = ureg[k];
     }
-    ureg[k] = v;
-    sm.u[k * L2 + tid] = v;
+    sm.u[k * L2 + tid] = ureg[k];
   }
   __syncthreads();
   float Di[LX], Dj[LX];
@@ -735,27 +790,32 @@ __global__ void __launch_bounds__(LX * LX)
       if (MODE == 2) freg[k] = a.f[id];
     }
   }
-  double ureg[LX];
+  double ureg[LX], pold[LX];
   const double beta = (MODE == 1 && !a.first) ? a.sc->beta : 0.0;
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {  // all loads before the first store
+    const size_t id = base + size_t(k) * L2 + t;
+    if (MODE == 1) {
+      ureg[k] = a.u[id];
+      pold[k] = a.first ? 0.0 : a.p[id];
+    } else if (MODE == 2) {
+      ureg[k] = a.p[id];
+      pold[k] = a.e ? double(a.e[id]) : 0.0;
+    } else {
+      ureg[k] = a.u[id];
+    }
+  }
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const size_t id = base + size_t(k) * L2 + t;
-    double v;
     if (MODE == 1) {
-      const double z = a.u[id];
-      v = a.first ? z : fma_rn(beta, a.p[id], z);  // add2s1, math.f:534
-      a.p[id] = v;
-    } else if (MODE == 2) {
-      v = a.p[id];
-      if (a.e) {
-        v = fma_rn(a.scale, double(a.e[id]), v);
-        a.p[id] = v;
-      }
-    } else {
-      v = a.u[id];
+      if (!a.first) ureg[k] = fma_rn(beta, pold[k], ureg[k]);  // add2s1, math.f:534
+      a.p[id] = ureg[k];
+    } else if (MODE == 2 && a.e) {
+      ureg[k] = fma_rn(a.scale, pold[k], ureg[k]);
+      a.p[id] = ureg[k];
     }
-    ureg[k] = v;
-    sm.A[eo_at<LX>(i, j, k)] = v;
+    sm.A[eo_at<LX>(i, j, k)] = ureg[k];
   }
   __syncthreads();
 
