@@ -159,10 +159,18 @@ int  nb_mesh_info(const nb_mesh *mesh, int *nelt, int *lx1, int *fused);
  * [-1,1] per global point, dssum'd, times c, masked. */
 int nb_setup_g(nb_mesh *mesh, double *g);
 int nb_set_multiplicity(nb_mesh *mesh, double *c);
+/* Geometric factors of the box with every element the trilinear image of
+ * its vertices, each vertex displaced by amp*h*sum_{q<4} a_q sin(k_q.X +
+ * phi_q) (h = 2, the reference element's size; mode parameters from
+ * splitmix64(seed)).  No counterpart in the reference, whose elements are
+ * undeformed (prox_setup.f:27-52). */
+int nb_setup_g_deformed(nb_mesh *mesh, double *g, uint64_t seed, double amp);
 int nb_rhs_uniform(nb_mesh *mesh, double *f, const double *c, uint64_t seed);
 
 /* w = A u on the device (FP64) */
 int nb_ax(nb_mesh *mesh, double *w, const double *u, const double *g);
+/* w = A u with the FP32 operator (FP32 u, w and g of 6n floats) */
+int nb_ax_f32(nb_mesh *mesh, float *w, const float *u, const float *g);
 /* dssum on a device vector (dom 1 double, 2 float) */
 int nb_dssum(nb_mesh *mesh, void *u, int dom);
 

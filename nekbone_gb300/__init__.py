@@ -40,7 +40,7 @@ EXPORTS = (
     "nekbone_set_error_mode", "nekbone_version", "nekbone_common_",
     "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
     "nekbone_get_flops_", "nekbone_set_flops_", "nekbone_set_contraction_order_",
-    "nb_mesh_set_order", "gs_setup_", "gs_op_",
+    "nb_mesh_set_order", "nb_setup_g_deformed", "nb_ax_f32", "gs_setup_", "gs_op_",
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
@@ -60,6 +60,10 @@ for _name in ("nb_mesh_create", "nb_mesh_destroy", "nb_mesh_info", "nb_setup_g",
               "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync"):
     getattr(lib, _name).restype = _i
 lib.nb_mesh_npts.argtypes = [_p]
+lib.nb_setup_g_deformed.restype = _i
+lib.nb_setup_g_deformed.argtypes = [_p, _p, _C.c_uint64, _d]
+lib.nb_ax_f32.restype = _i
+lib.nb_ax_f32.argtypes = [_p, _p, _p, _p]
 lib.nb_mesh_set_order.restype = _i
 lib.nb_mesh_set_order.argtypes = [_p, _i]
 lib.nb_mesh_destroy.argtypes = [_p]
@@ -366,6 +370,12 @@ class DeviceMesh:
 
     def setup_g(self, g_ptr: int) -> None:
         _check(lib.nb_setup_g(self._h, _p(g_ptr)))
+
+    def setup_g_deformed(self, g_ptr: int, seed: int, amp: float = 0.1) -> None:
+        _check(lib.nb_setup_g_deformed(self._h, _p(g_ptr), seed, amp))
+
+    def ax_f32(self, w_ptr: int, u_ptr: int, g_ptr: int) -> None:
+        _check(lib.nb_ax_f32(self._h, _p(w_ptr), _p(u_ptr), _p(g_ptr)))
 
     def set_multiplicity(self, c_ptr: int) -> None:
         _check(lib.nb_set_multiplicity(self._h, _p(c_ptr)))

@@ -33,6 +33,8 @@ int dev_local_grad3_t(double *u, const double *ur, const double *us,
 int dev_setup_g(const Operator &op, double *g, cudaStream_t s);
 int dev_rhs_uniform(const Operator &op, double *f, const double *c,
                     uint64_t seed, cudaStream_t s);
+int dev_setup_g_deformed(const Operator &op, double *g, uint64_t seed, double amp,
+                         cudaStream_t s);
 int dev_residual(const Operator &op, double *r, const double *f,
                  const double *w, long n, cudaStream_t s);
 int dev_axpy_f32(double *x, const float *e, double scale, long n, cudaStream_t s);
@@ -732,6 +734,19 @@ int nb_setup_g(nb_mesh *mesh, double *g) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
   NB_TRY(dev_setup_g(mesh->op, g, st().s));
+  return NB_OK;
+}
+
+int nb_setup_g_deformed(nb_mesh *mesh, double *g, uint64_t seed, double amp) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  return dev_setup_g_deformed(mesh->op, g, seed, amp, st().s);
+}
+
+int nb_ax_f32(nb_mesh *mesh, float *w, const float *u, const float *g) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  NB_TRY(apply_ax<float>(mesh->op, w, u, g, st().s));
   return NB_OK;
 }
 
