@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-sample-nel", type=int, default=16)
     ap.add_argument("--cpu-sample-iters", type=int, default=100)
@@ -167,6 +168,64 @@ def run_reference(a, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- extras --
+def extras(nb, torch, dev):
+    """Deformed-geometry operator error per lx1 (16^3 elements) and
+    hsmg-preconditioned CG against plain CG (16^3 deformed, lx1=12,
+    levels 12 -> 6 -> 3), to relative residual 1e-10."""
+    res = {"deformed_operator_error": {}, "hsmg_pcg": {}}
+    for lx in (8, 12, 16):
+        m = nb.DeviceMesh(16, 16, 16, lx, mask_mode=1)
+        n = m.n
+        g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+        m.setup_g_deformed(g.data_ptr(), 11, 0.1)
+        u = torch.rand(n, dtype=torch.float64, device=dev) * 2 - 1
+        m.dssum(u.data_ptr(), 1)        # continuous field
+        w64 = torch.empty_like(u)
+        m.set_order(0)
+        m.ax(w64.data_ptr(), u.data_ptr(), g.data_ptr())
+        m.set_order(1)
+        w32 = torch.empty(n, dtype=torch.float32, device=dev)
+        u32, g32 = u.float(), g.float()
+        m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())
+        torch.cuda.synchronize()
+        d = (w32.double() - w64).abs().max().item() / w64.abs().max().item()
+        res["deformed_operator_error"][f"lx1={lx}"] = {"fp32": d, "n": n}
+        del g, u, w64, w32, u32, g32
+        m.close()
+        torch.cuda.empty_cache()
+    m = nb.DeviceMesh(16, 16, 16, 12, mask_mode=1)
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g_deformed(g.data_ptr(), 11, 0.1)
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 5)
+    x = torch.zeros_like(f)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    it, rr = m.cg_tol(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), 1e-10,
+                      max_iter=20000, check_every=10)
+    tcg = time.perf_counter() - t0
+    res["hsmg_pcg"]["cg"] = {"iters": it, "relres": rr, "s": tcg}
+    for prec in (32, 64):
+        t0 = time.perf_counter()
+        m.mg_setup([2, 5, 11], precision=prec)
+        tset = time.perf_counter() - t0
+        x.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, rr = m.pcg_tol(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), 1e-10,
+                           max_iter=2000, check_every=2)
+        tp = time.perf_counter() - t0
+        res["hsmg_pcg"][f"pcg_fp{prec}_smoother"] = {"iters": it, "relres": rr, "s": tp,
+                                                     "setup_s": tset}
+    res["hsmg_pcg"]["workload"] = "16^3 deformed elements, lx1=12, levels 12->6->3, tol 1e-10"
+    m.close()
+    return res
 
 
 # --------------------------------------------------------------- GPU arm --
@@ -282,9 +341,16 @@ def run_ours(a, rank, world, local):
                         "mixed_relres": rrm, "speedup": t64 / tm, "x_rel_diff": diff}
         del xt, xm
 
+    # ---- the other workloads, one measurement each (not the headline)
+    if not a.no_extras and world == 1:
+        del x, r, w, p, z
+        torch.cuda.empty_cache()
+        out["extras"] = extras(nb, torch, dev)
+        x = r = w = p = z = None
+
     # ---- end to end through the drop-in cg_ with pinned host buffers
     if not a.no_e2e:
-        del x, r, w, p, z
+        x = r = w = p = z = None
         torch.cuda.empty_cache()
         hb = nb.Nekbone(nel, nel, nel, lx, mask_mode=1)
         pin = lambda t: t.cpu().pin_memory()

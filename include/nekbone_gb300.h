@@ -216,6 +216,21 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
 int nb_glsc3_noalloc(const double *a, const double *b, const double *mult,
                      long n, double *result, void *stream);
 
+/* hsmg on the device mesh.  orders: nlev polynomial orders, coarsest first,
+ * the last lx1-1 (NULL = the reference's level choice, hsmg.f:45-97, lx1 <=
+ * 10).  precision 64 = FP64 throughout (h1mg_solve's arithmetic); 32 = the
+ * Schwarz smoother, restriction and interpolation in FP32, the coarse solve
+ * in FP64. */
+int nb_mg_setup(nb_mesh *mesh, const int *orders, int nlev, int precision);
+/* z = M^-1 rhs (h1mg_solve, hsmg.f:960-1034); masks rhs in place */
+int nb_mg_solve(nb_mesh *mesh, double *z, double *rhs);
+/* FP64 CG preconditioned with the mesh's hsmg until
+ * sqrt(r'Cr)/sqrt(r0'Cr0) <= tol (max_iter cap; residual polled every
+ * check_every iterations). */
+int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
+               const double *c, double tol, int max_iter, int check_every,
+               int *iters, double *relres);
+
 /* Synchronise the library's stream. */
 int nb_sync(void);
 /* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for

@@ -40,7 +40,8 @@ EXPORTS = (
     "nekbone_set_error_mode", "nekbone_version", "nekbone_common_",
     "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
     "nekbone_get_flops_", "nekbone_set_flops_", "nekbone_set_contraction_order_",
-    "nb_mesh_set_order", "nb_setup_g_deformed", "nb_ax_f32", "gs_setup_", "gs_op_",
+    "nb_mesh_set_order", "nb_setup_g_deformed", "nb_ax_f32", "nb_mg_setup",
+    "nb_mg_solve", "nb_pcg_tol", "gs_setup_", "gs_op_",
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
@@ -60,6 +61,12 @@ for _name in ("nb_mesh_create", "nb_mesh_destroy", "nb_mesh_info", "nb_setup_g",
               "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync"):
     getattr(lib, _name).restype = _i
 lib.nb_mesh_npts.argtypes = [_p]
+lib.nb_mg_setup.restype = _i
+lib.nb_mg_setup.argtypes = [_p, _p, _i, _i]
+lib.nb_mg_solve.restype = _i
+lib.nb_mg_solve.argtypes = [_p, _p, _p]
+lib.nb_pcg_tol.restype = _i
+lib.nb_pcg_tol.argtypes = [_p, _p, _p, _p, _p, _d, _i, _i, _p, _p]
 lib.nb_setup_g_deformed.restype = _i
 lib.nb_setup_g_deformed.argtypes = [_p, _p, _C.c_uint64, _d]
 lib.nb_ax_f32.restype = _i
@@ -418,6 +425,22 @@ class DeviceMesh:
         _check(lib.nb_time_cg_kernels_f32(self._h, _p(x), _p(f), _p(g), _p(c), _p(r),
                                           _p(w), _p(p), reps, _ptr(ms)))
         return ms
+
+    def mg_setup(self, orders=None, precision: int = 64) -> None:
+        if orders is None:
+            _check(lib.nb_mg_setup(self._h, None, 0, precision))
+        else:
+            o = _np.ascontiguousarray(orders, dtype=_np.int32)
+            _check(lib.nb_mg_setup(self._h, _ptr(o), len(o), precision))
+
+    def mg_solve(self, z, rhs) -> None:
+        _check(lib.nb_mg_solve(self._h, _p(z), _p(rhs)))
+
+    def pcg_tol(self, x, f, g, c, tol: float, max_iter: int = 5000, check_every: int = 5):
+        it, rr = _C.c_int(), _C.c_double()
+        _check(lib.nb_pcg_tol(self._h, _p(x), _p(f), _p(g), _p(c), tol, max_iter,
+                              check_every, _C.byref(it), _C.byref(rr)))
+        return it.value, rr.value
 
     def cg_tol(self, x, f, g, c, tol: float, max_iter: int = 20000, check_every: int = 25):
         it, rr = _C.c_int(), _C.c_double()

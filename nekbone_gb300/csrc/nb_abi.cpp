@@ -851,6 +851,64 @@ int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
                                   ms3, lib_stream());
 }
 
+int nb_mg_setup(nb_mesh *mesh, const int *orders, int nlev, int precision) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  std::unique_ptr<Multigrid> mg(new Multigrid());
+  NB_TRY(mg_setup(mg.get(), mesh->op, orders, nlev, st().s, precision));
+  mesh->mg = std::move(mg);
+  return NB_OK;
+}
+
+int nb_mg_solve(nb_mesh *mesh, double *z, double *rhs) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (!mesh->mg) return fail(NB_ERR_STATE, "nb_mg_solve: call nb_mg_setup first");
+  return mg_solve(*mesh->mg, z, rhs, st().s);
+}
+
+int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
+               const double *c, double tol, int max_iter, int check_every,
+               int *iters, double *relres) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (!mesh->mg) return fail(NB_ERR_STATE, "nb_pcg_tol: call nb_mg_setup first");
+  cudaStream_t s = lib_stream();
+  Operator &op = mesh->op;
+  CgWork &wk = mesh->wk;
+  const long n = op.n;
+  if (check_every < 1) check_every = 1;
+  double *r = nullptr, *w = nullptr, *p = nullptr, *z = nullptr;
+  NB_CUDA(cudaMalloc(&r, n * 8));
+  NB_CUDA(cudaMalloc(&w, n * 8));
+  NB_CUDA(cudaMalloc(&p, n * 8));
+  NB_CUDA(cudaMalloc(&z, n * 8));
+  MgPrecond M(mesh->mg.get());
+  int done = 0, stt = NB_OK;
+  double rn0 = 0.0, rn = 0.0;
+  stt = cg_begin(op, wk, x, f, c, r, max_iter, s);
+  if (!stt && cudaMemcpy(&rn0, &wk.sc->rnorm, 8, cudaMemcpyDeviceToHost) != cudaSuccess)
+    stt = fail(NB_ERR_CUDA, "nb_pcg_tol: reading rnorm");
+  rn = rn0;
+  while (!stt && done < max_iter) {
+    const int k = std::min(check_every, max_iter - done);
+    stt = cg_steps_pc(op, wk, x, g, c, r, w, p, z, done + 1, done + k, &M, s);
+    done += k;
+    if (!stt && (cudaMemcpyAsync(&rn, &wk.sc->rnorm, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                 cudaStreamSynchronize(s) != cudaSuccess))
+      stt = fail(NB_ERR_CUDA, "nb_pcg_tol: reading rnorm");
+    if (rn0 > 0 && rn / rn0 <= tol) break;
+  }
+  cudaFree(r);
+  cudaFree(w);
+  cudaFree(p);
+  cudaFree(z);
+  if (stt) return stt;
+  if (iters) *iters = done;
+  if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
+  return NB_OK;
+}
+
 int nb_sync(void) {
   clear_status();
   if (st().init()) return last_status();

@@ -28,10 +28,17 @@ Multigrid::~Multigrid() {
     for (double *p : ps)
       if (p) cudaFree(p);
     if (L.mask) cudaFree(L.mask);
+    float *pf[] = {L.rstr_wt_f, L.fast_s_f, L.fast_d_f, L.schwarz_wt_f, L.jh_f, L.jht_f,
+                   L.e_f, L.r_f};
+    for (float *p : pf)
+      if (p) cudaFree(p);
   }
   if (A) cudaFree(A);
   if (B) cudaFree(B);
   if (w) cudaFree(w);
+  if (A_f) cudaFree(A_f);
+  if (B_f) cudaFree(B_f);
+  if (z_f) cudaFree(z_f);
 }
 
 namespace {
@@ -40,36 +47,38 @@ namespace {
 // v(nv^3) = [Ct (x) Bt (x) A] u(nu^3): work = A u, work2 = work Bt per slab,
 // v = work2 Ct.  A is nv x nu, Bt and Ct are nu x nv, column-major.  All
 // operands in shared memory, the CTA cooperates; ends with a barrier.
-__device__ void tensor3(double *v, const double *u, int nv, int nu,
-                        const double *A, const double *Bt, const double *Ct,
-                        double *work, double *work2) {
+// T is the working precision (FP64, or FP32 for the FP32 smoother).
+template <typename T>
+__device__ void tensor3(T *v, const T *u, int nv, int nu, const T *A, const T *Bt,
+                        const T *Ct, T *work, T *work2) {
   const int t = threadIdx.x, nt = blockDim.x;
   const int nu2 = nu * nu;
   for (int q = t; q < nv * nu2; q += nt) {  // work(a, n p) = sum_m A(a,m) u(m, n p)
     const int a = q % nv, np_ = q / nv;
-    double s = mul_rn(A[a], u[np_ * nu]);
+    T s = mul_rn(A[a], u[np_ * nu]);
     for (int m = 1; m < nu; ++m) s = fma_rn(A[a + m * nv], u[m + np_ * nu], s);
     work[q] = s;
   }
   __syncthreads();
   for (int q = t; q < nv * nv * nu; q += nt) {  // work2(a,b,p) = sum_n work(a,n,p) Bt(n,b)
     const int a = q % nv, b = (q / nv) % nv, p = q / (nv * nv);
-    const double *wp = work + nv * nu * p;
-    double s = mul_rn(wp[a], Bt[b * nu]);
+    const T *wp = work + nv * nu * p;
+    T s = mul_rn(wp[a], Bt[b * nu]);
     for (int n = 1; n < nu; ++n) s = fma_rn(wp[a + n * nv], Bt[n + b * nu], s);
     work2[q] = s;
   }
   __syncthreads();
   for (int q = t; q < nv * nv * nv; q += nt) {  // v(ab, c) = sum_p work2(ab,p) Ct(p,c)
     const int ab = q % (nv * nv), c = q / (nv * nv);
-    double s = mul_rn(work2[ab], Ct[c * nu]);
+    T s = mul_rn(work2[ab], Ct[c * nu]);
     for (int p = 1; p < nu; ++p) s = fma_rn(work2[ab + p * nv * nv], Ct[p + c * nu], s);
     v[q] = s;
   }
   __syncthreads();
 }
 
-__device__ inline void load_shared(double *dst, const double *src, int n) {
+template <typename T>
+__device__ inline void load_shared(T *dst, const T *src, int n) {
   for (int q = threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
 }
 
@@ -87,7 +96,8 @@ __device__ inline int ghost_face(int a, int b, int c, int nl) {
 // h1mg_schwarz_toext3d + extrude(A,0,0,A,2,1) (hsmg.f:1075-1077): regular
 // points copied into the extended array, each ghost face set to the
 // element's own layer-2 value, ghost edges and corners zero.
-__global__ void k_toext(double *A, const double *r, int nh, int nelt) {
+template <typename T>
+__global__ void k_toext(T *A, const T *r, int nh, int nelt) {
   const int nl = nh + 2;
   const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh;
   const long tot = nl3 * nelt;
@@ -97,7 +107,7 @@ __global__ void k_toext(double *A, const double *r, int nh, int nelt) {
     const int rr = int(q % nl3);
     int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
     const int gf = ghost_face(a, b, c, nl);
-    double v = 0.0;
+    T v = T(0);
     if (a >= 1 && a <= nh && b >= 1 && b <= nh && c >= 1 && c <= nh) {
       v = r[e * nh3 + (a - 1) + nh * (b - 1) + long(nh) * nh * (c - 1)];
     } else if (gf) {
@@ -112,7 +122,8 @@ __global__ void k_toext(double *A, const double *r, int nh, int nelt) {
 
 // extrude(A,0,1,A,2,-1) (hsmg.f:1079): ghost faces minus the own layer-2
 // value, leaving the neighbour's value
-__global__ void k_ghost_minus(double *A, int nh, int nelt) {
+template <typename T>
+__global__ void k_ghost_minus(T *A, int nh, int nelt) {
   const int nl = nh + 2;
   const long nl3 = long(nl) * nl * nl, tot = nl3 * nelt;
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
@@ -125,30 +136,31 @@ __global__ void k_ghost_minus(double *A, int nh, int nelt) {
     else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
     else if (gf == 5) c = 2; else c = nl - 3;
     const long p = q - rr + a + long(nl) * b + long(nl) * nl * c;
-    A[q] = fma_rn(-1.0, A[p], A[q]);
+    A[q] = fma_rn(T(-1), A[p], A[q]);
   }
 }
 
 // h1mg_do_fast (hsmg.f:1297-1318): B = S (d .* (S^T A)) per extended element;
 // also saves B's ghost faces into A (the first extrude of the overlap sum,
 // hsmg.f:1084: A <- 0*A + B on the ghost faces).
-__global__ void k_fdm(double *B, double *A, const double *s, const double *d,
-                      int nl) {
-  extern __shared__ double sm[];
+template <typename T>
+__global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
   const int nl2 = nl * nl, nl3 = nl2 * nl;
-  double *u = sm, *v = u + nl3, *work = v + nl3, *work2 = work + nl3,
-         *S = work2 + nl3;  // 6 matrices nl*nl
+  T *u = sm, *v = u + nl3, *work = v + nl3, *work2 = work + nl3,
+    *S = work2 + nl3;  // 6 matrices nl*nl
   const long e = blockIdx.x;
   load_shared(u, A + e * nl3, nl3);
   load_shared(S, s + e * 6L * nl2, 6 * nl2);
   __syncthreads();
   // s(1,2,1)=S_r^T, s(1,1,2)=S_s, s(1,1,3)=S_t
-  tensor3(v, u, nl, nl, S + nl2, S + 2 * nl2, S + 4 * nl2, work, work2);
-  const double *de = d + e * nl3;
+  tensor3<T>(v, u, nl, nl, S + nl2, S + 2 * nl2, S + 4 * nl2, work, work2);
+  const T *de = d + e * nl3;
   for (int q = threadIdx.x; q < nl3; q += blockDim.x) u[q] = mul_rn(de[q], v[q]);
   __syncthreads();
   // s(1,1,1)=S_r, s(1,2,2)=S_s^T, s(1,2,3)=S_t^T
-  tensor3(v, u, nl, nl, S, S + 3 * nl2, S + 5 * nl2, work, work2);
+  tensor3<T>(v, u, nl, nl, S, S + 3 * nl2, S + 5 * nl2, work, work2);
   for (int q = threadIdx.x; q < nl3; q += blockDim.x) {
     const int a = q % nl, b = (q / nl) % nl, c = q / nl2;
     B[e * nl3 + q] = v[q];
@@ -160,8 +172,8 @@ __global__ void k_fdm(double *B, double *A, const double *s, const double *d,
 // each regular point adds, in the reference's face order, the neighbour
 // contributions (gs'd ghost minus saved ghost) of the ghost faces whose
 // layer-2 partner it is.
-__global__ void k_overlap_toreg(double *e_out, const double *B, const double *A,
-                                int nh, int nelt) {
+template <typename T>
+__global__ void k_overlap_toreg(T *e_out, const T *B, const T *A, int nh, int nelt) {
   const int nl = nh + 2;
   const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh, tot = nh3 * nelt;
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
@@ -171,40 +183,41 @@ __global__ void k_overlap_toreg(double *e_out, const double *B, const double *A,
     const int a = rr % nh + 1, b = (rr / nh) % nh + 1, c = rr / (nh * nh) + 1;
     const long base = e * nl3;
     auto at = [&](int x, int y, int z) { return base + x + long(nl) * y + long(nl) * nl * z; };
-    double v = B[at(a, b, c)];
-    if (a == 2) { const long g = at(0, b, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
-    if (a == nl - 3) { const long g = at(nl - 1, b, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
-    if (b == 2) { const long g = at(a, 0, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
-    if (b == nl - 3) { const long g = at(a, nl - 1, c); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
-    if (c == 2) { const long g = at(a, b, 0); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
-    if (c == nl - 3) { const long g = at(a, b, nl - 1); v = add_rn(v, fma_rn(-1.0, A[g], B[g])); }
+    T v = B[at(a, b, c)];
+    if (a == 2) { const long g = at(0, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (a == nl - 3) { const long g = at(nl - 1, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (b == 2) { const long g = at(a, 0, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (b == nl - 3) { const long g = at(a, nl - 1, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (c == 2) { const long g = at(a, b, 0); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (c == nl - 3) { const long g = at(a, b, nl - 1); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
     e_out[q] = v;
   }
 }
 
 // h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps
-__global__ void k_schwarz_wt(double *e, const double *wt, int n, int nelt) {
+template <typename T>
+__global__ void k_schwarz_wt(T *e, const T *wt, int n, int nelt) {
   const long n3 = long(n) * n * n, tot = n3 * nelt;
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
        q += long(gridDim.x) * blockDim.x) {
     const long el = q / n3;
     const int rr = int(q % n3);
     const int i = rr % n, j = (rr / n) % n, k = rr / (n * n);
-    const double *we = wt + el * 12L * n * n;
+    const T *we = wt + el * 12L * n * n;
     auto W = [&](int a, int b, int s, int d) {
       return we[a + n * b + n * n * s + 4 * n * n * d];
     };
     const int L[4] = {0, 1, n - 2, n - 1};
-    double v = e[q];
+    T v = e[q];
     bool done = false;
     for (int s = 0; s < 4; ++s)
-      if (i == L[s]) { v = mul_rn(v, sqrt(W(j, k, s, 0))); done = true; }
+      if (i == L[s]) { v = mul_rn(v, T(sqrt(W(j, k, s, 0)))); done = true; }
     if (!done && i >= 2 && i <= n - 3) {
       for (int s = 0; s < 4; ++s)
-        if (j == L[s]) { v = mul_rn(v, sqrt(W(i, k, s, 1))); done = true; }
+        if (j == L[s]) { v = mul_rn(v, T(sqrt(W(i, k, s, 1)))); done = true; }
       if (!done && j >= 2 && j <= n - 3)
         for (int s = 0; s < 4; ++s)
-          if (k == L[s]) v = mul_rn(v, sqrt(W(i, j, s, 2)));
+          if (k == L[s]) v = mul_rn(v, T(sqrt(W(i, j, s, 2))));
     }
     e[q] = v;
   }
@@ -212,17 +225,19 @@ __global__ void k_schwarz_wt(double *e, const double *wt, int n, int nelt) {
 
 // h1mg_rstr (hsmg.f:1340-1360): do_wt (hsmg.f:1362-1391) then
 // v = [J^T (x) J^T (x) J^T] u per element
-__global__ void k_rstr(double *v, const double *u, const double *wt, int nu,
-                       int nv, const double *jht, const double *jh) {
-  extern __shared__ double sm[];
+template <typename T>
+__global__ void k_rstr(T *v, const T *u, const T *wt, int nu, int nv, const T *jht,
+                       const T *jh) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
   const int nu3 = nu * nu * nu, nmax = max(nu, nv), nmax3 = nmax * nmax * nmax;
-  double *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3,
-         *Jt = work2 + nmax3, *J = Jt + nu * nv;
+  T *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3,
+    *Jt = work2 + nmax3, *J = Jt + nu * nv;
   const long e = blockIdx.x;
-  const double *we = wt + e * 6L * nu * nu;
+  const T *we = wt + e * 6L * nu * nu;
   for (int q = threadIdx.x; q < nu3; q += blockDim.x) {
     const int i = q % nu, j = (q / nu) % nu, k = q / (nu * nu);
-    double x = u[e * nu3 + q];
+    T x = u[e * nu3 + q];
     if (i == 0) x = mul_rn(x, we[j + nu * k + 0]);
     else if (i == nu - 1) x = mul_rn(x, we[j + nu * k + nu * nu]);
     else if (j == 0) x = mul_rn(x, we[i + nu * k + 2 * nu * nu]);
@@ -234,25 +249,26 @@ __global__ void k_rstr(double *v, const double *u, const double *wt, int nu,
   load_shared(Jt, jht, nu * nv);
   load_shared(J, jh, nu * nv);
   __syncthreads();
-  tensor3(vs, us, nv, nu, Jt, J, J, work, work2);
+  tensor3<T>(vs, us, nv, nu, Jt, J, J, work, work2);
   const int nv3 = nv * nv * nv;
   for (int q = threadIdx.x; q < nv3; q += blockDim.x) v[e * nv3 + q] = vs[q];
 }
 
 // h1mg_intp (hsmg.f:1436-1475) accumulated: out += [J (x) J (x) J] uc
-__global__ void k_intp_add(double *out, const double *uc, int nu, int nv,
-                           const double *jh, const double *jht) {
-  extern __shared__ double sm[];
+template <typename T>
+__global__ void k_intp_add(T *out, const T *uc, int nu, int nv, const T *jh, const T *jht) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
   const int nmax = max(nu, nv), nmax3 = nmax * nmax * nmax;
-  double *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3,
-         *J = work2 + nmax3, *Jt = J + nu * nv;
+  T *us = sm, *vs = us + nmax3, *work = vs + nmax3, *work2 = work + nmax3, *J = work2 + nmax3,
+    *Jt = J + nu * nv;
   const long e = blockIdx.x;
   const int nu3 = nu * nu * nu, nv3 = nv * nv * nv;
   load_shared(us, uc + e * nu3, nu3);
   load_shared(J, jh, nu * nv);
   load_shared(Jt, jht, nu * nv);
   __syncthreads();
-  tensor3(vs, us, nv, nu, J, Jt, Jt, work, work2);
+  tensor3<T>(vs, us, nv, nu, J, Jt, Jt, work, work2);
   for (int q = threadIdx.x; q < nv3; q += blockDim.x)
     out[e * nv3 + q] = add_rn(out[e * nv3 + q], vs[q]);
 }
@@ -472,16 +488,32 @@ int overlap_sum(const MgLevel &L, int nelt, double *e, double *B, double *A,
                 cudaStream_t s) {
   k_save_ghost<<<grid_for(L.next), 256, 0, s>>>(A, B, L.nl, nelt);
   NB_TRY(gs_exec(L.gsx, B, 1, 1, 0, s));
-  k_overlap_toreg<<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
+  k_overlap_toreg<double><<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
 
 }  // namespace
 
+__global__ void k_to_f32(float *y, const double *x, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    y[q] = float(x[q]);
+}
+
+int copy_f32(float **dst, const double *src, long n, cudaStream_t s) {
+  NB_TRY(dmalloc(dst, size_t(n)));
+  k_to_f32<<<grid_for(n), 256, 0, s>>>(*dst, src, n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
 int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
-             cudaStream_t s) {
+             cudaStream_t s, int precision) {
+  if (precision != 64 && precision != 32)
+    return fail(NB_ERR_ARG, "h1mg: precision %d not 64 or 32", precision);
   mg->op = &op;
+  mg->precision = precision;
   const int nx1 = op.lx, nelt = op.nelt;
   int ord[8] = {0};
   if (!orders) {
@@ -631,75 +663,174 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
   const size_t sm_fdm = sizeof(double) * (4 * size_t(maxnl) * maxnl * maxnl + 6 * maxnl * maxnl);
   if (sm_fdm > 227 * 1024)
     return fail(NB_ERR_UNSUPPORTED, "h1mg: extended element of %d points too large", maxnl);
-  NB_TRY(set_smem((const void *)k_fdm, sm_fdm));
-  NB_TRY(set_smem((const void *)k_rstr, tensor_smem(maxnl, 2 * maxnl * maxnl)));
-  NB_TRY(set_smem((const void *)k_intp_add, tensor_smem(maxnl, 2 * maxnl * maxnl)));
+  NB_TRY(set_smem((const void *)k_fdm<double>, sm_fdm));
+  NB_TRY(set_smem((const void *)k_rstr<double>, tensor_smem(maxnl, 2 * maxnl * maxnl)));
+  NB_TRY(set_smem((const void *)k_intp_add<double>, tensor_smem(maxnl, 2 * maxnl * maxnl)));
+  NB_TRY(set_smem((const void *)k_fdm<float>, sm_fdm / 2));
+  NB_TRY(set_smem((const void *)k_rstr<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
+  NB_TRY(set_smem((const void *)k_intp_add<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
+  if (precision == 32) {
+    for (int l = 1; l <= nlev; ++l) {
+      MgLevel &L = mg->lv[l];
+      NB_TRY(copy_f32(&L.rstr_wt_f, L.rstr_wt, long(L.nh) * L.nh * 6 * nelt, s));
+      if (l >= 2) {
+        NB_TRY(copy_f32(&L.fast_s_f, L.fast_s, long(L.nl) * L.nl * 6 * nelt, s));
+        NB_TRY(copy_f32(&L.fast_d_f, L.fast_d, long(L.nl) * L.nl * L.nl * nelt, s));
+        NB_TRY(copy_f32(&L.schwarz_wt_f, L.schwarz_wt, long(L.nh) * L.nh * 12 * nelt, s));
+      }
+      if (l < nlev) {
+        const long nfc = long(mg->lv[l + 1].nh) * L.nh;
+        NB_TRY(copy_f32(&L.jh_f, L.jh, nfc, s));
+        NB_TRY(copy_f32(&L.jht_f, L.jht, nfc, s));
+      }
+      NB_TRY(dmalloc(&L.e_f, L.n));
+      NB_TRY(dmalloc(&L.r_f, L.n));
+    }
+    NB_TRY(dmalloc(&mg->A_f, maxext));
+    NB_TRY(dmalloc(&mg->B_f, maxext));
+    NB_TRY(dmalloc(&mg->z_f, op.n));
+  }
   NB_CUDA(cudaStreamSynchronize(s));
   return NB_OK;
 }
 
 namespace {
 
+// Per-precision views of the level data.
+template <typename T>
+struct LevelView;
+template <>
+struct LevelView<double> {
+  static const double *rstr_wt(const MgLevel &L) { return L.rstr_wt; }
+  static const double *fast_s(const MgLevel &L) { return L.fast_s; }
+  static const double *fast_d(const MgLevel &L) { return L.fast_d; }
+  static const double *schwarz_wt(const MgLevel &L) { return L.schwarz_wt; }
+  static const double *jh(const MgLevel &L) { return L.jh; }
+  static const double *jht(const MgLevel &L) { return L.jht; }
+  static double *e(MgLevel &L) { return L.e; }
+  static double *r(MgLevel &L) { return L.r; }
+  static double *A(Multigrid &m) { return m.A; }
+  static double *B(Multigrid &m) { return m.B; }
+  static constexpr int dom = 1;
+};
+template <>
+struct LevelView<float> {
+  static const float *rstr_wt(const MgLevel &L) { return L.rstr_wt_f; }
+  static const float *fast_s(const MgLevel &L) { return L.fast_s_f; }
+  static const float *fast_d(const MgLevel &L) { return L.fast_d_f; }
+  static const float *schwarz_wt(const MgLevel &L) { return L.schwarz_wt_f; }
+  static const float *jh(const MgLevel &L) { return L.jh_f; }
+  static const float *jht(const MgLevel &L) { return L.jht_f; }
+  static float *e(MgLevel &L) { return L.e_f; }
+  static float *r(MgLevel &L) { return L.r_f; }
+  static float *A(Multigrid &m) { return m.A_f; }
+  static float *B(Multigrid &m) { return m.B_f; }
+  static constexpr int dom = 2;
+};
+
 // h1mg_schwarz (hsmg.f:1036-1051) at level l: e = sqrt(W) part1(r); masks r
-int mg_schwarz(Multigrid &mg, double *e, double *r, int l, cudaStream_t s) {
+template <typename T>
+int mg_schwarz(Multigrid &mg, T *e, T *r, int l, cudaStream_t s) {
+  typedef LevelView<T> V;
   MgLevel &L = mg.lv[l];
   const int nelt = mg.op->nelt;
-  NB_TRY(vec_mask<double>(r, L.mask, L.nmask, s));
-  k_toext<<<grid_for(L.next), 256, 0, s>>>(mg.A, r, L.nh, nelt);
-  NB_TRY(gs_exec(L.gsx, mg.A, 1, 1, 0, s));
-  k_ghost_minus<<<grid_for(L.next), 256, 0, s>>>(mg.A, L.nh, nelt);
+  T *A = V::A(mg), *B = V::B(mg);
+  NB_TRY(vec_mask<T>(r, L.mask, L.nmask, s));
+  k_toext<T><<<grid_for(L.next), 256, 0, s>>>(A, r, L.nh, nelt);
+  NB_TRY(gs_exec(L.gsx, A, V::dom, 1, 0, s));
+  k_ghost_minus<T><<<grid_for(L.next), 256, 0, s>>>(A, L.nh, nelt);
   const int nl = L.nl;
-  const size_t sm = sizeof(double) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
-  k_fdm<<<nelt, 256, sm, s>>>(mg.B, mg.A, L.fast_s, L.fast_d, nl);
+  const size_t sm = sizeof(T) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
+  k_fdm<T><<<nelt, 256, sm, s>>>(B, A, V::fast_s(L), V::fast_d(L), nl);
   NB_CUDA(cudaGetLastError());
-  NB_TRY(gs_exec(L.gsx, mg.B, 1, 1, 0, s));
-  k_overlap_toreg<<<grid_for(L.n), 256, 0, s>>>(e, mg.B, mg.A, L.nh, nelt);
-  NB_TRY(gs_exec(L.gs, e, 1, 1, 0, s));
-  NB_TRY(vec_mask<double>(e, L.mask, L.nmask, s));
-  k_schwarz_wt<<<grid_for(L.n), 256, 0, s>>>(e, L.schwarz_wt, L.nh, nelt);
+  NB_TRY(gs_exec(L.gsx, B, V::dom, 1, 0, s));
+  k_overlap_toreg<T><<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
+  NB_TRY(gs_exec(L.gs, e, V::dom, 1, 0, s));
+  NB_TRY(vec_mask<T>(e, L.mask, L.nmask, s));
+  k_schwarz_wt<T><<<grid_for(L.n), 256, 0, s>>>(e, V::schwarz_wt(L), L.nh, nelt);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
 
-int mg_rstr(Multigrid &mg, double *rc, const double *rf, int l, bool dssum,
-            cudaStream_t s) {
+template <typename T>
+int mg_rstr(Multigrid &mg, T *rc, const T *rf, int l, bool dssum, cudaStream_t s) {
+  typedef LevelView<T> V;
   const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
   const int nmax = std::max(F.nh, C.nh);
-  k_rstr<<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh), s>>>(
-      rc, rf, F.rstr_wt, F.nh, C.nh, C.jht, C.jh);
+  k_rstr<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
+      rc, rf, V::rstr_wt(F), F.nh, C.nh, V::jht(C), V::jh(C));
   NB_CUDA(cudaGetLastError());
-  if (dssum) NB_TRY(gs_exec(C.gs, rc, 1, 1, 0, s));
+  if (dssum) NB_TRY(gs_exec(C.gs, rc, V::dom, 1, 0, s));
   return NB_OK;
 }
 
-int mg_intp_add(Multigrid &mg, double *of, const double *ec, int l, cudaStream_t s) {
+template <typename T>
+int mg_intp_add(Multigrid &mg, T *of, const T *ec, int l, cudaStream_t s) {
+  typedef LevelView<T> V;
   const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
   const int nmax = std::max(F.nh, C.nh);
-  k_intp_add<<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh), s>>>(
-      of, ec, C.nh, F.nh, C.jh, C.jht);
+  k_intp_add<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
+      of, ec, C.nh, F.nh, V::jh(C), V::jht(C));
   NB_CUDA(cudaGetLastError());
   return NB_OK;
+}
+
+__global__ void k_to_f64(double *y, const float *x, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    y[q] = double(x[q]);
+}
+
+// The V-cycle of h1mg_solve (hsmg.f:960-1034) in precision T from level Lm
+// down; the coarse "solve" (copy + dssum + mask, hsmg.f:945-957) is always
+// FP64.  rT is the top-level right-hand side (already masked), zT the result.
+template <typename T>
+int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
+  typedef LevelView<T> V;
+  const int Lm = mg.nlev;
+  MgLevel &Top = mg.lv[Lm];
+  NB_TRY(mg_schwarz<T>(mg, zT, rT, Lm, s));
+  T *rTop = V::r(Top);
+  if (rTop != rT) NB_TRY(vec_copy<T>(rTop, rT, Top.n, s));
+  for (int l = Lm - 1; l >= 2; --l) {
+    NB_TRY(mg_rstr<T>(mg, V::r(mg.lv[l]), V::r(mg.lv[l + 1]), l, true, s));
+    NB_TRY(mg_schwarz<T>(mg, V::e(mg.lv[l]), V::r(mg.lv[l]), l, s));
+  }
+  MgLevel &C = mg.lv[1];
+  NB_TRY(mg_rstr<T>(mg, V::r(C), V::r(mg.lv[2]), 1, false, s));
+  if (std::is_same<T, double>::value) {
+    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
+    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));  // hsmg_coarse_solve
+    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
+    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
+  } else {
+    // FP64 coarse solve between the FP32 legs
+    k_to_f64<<<grid_for(C.n), 256, 0, s>>>(C.r, C.r_f, C.n);
+    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
+    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));
+    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
+    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
+    k_to_f32<<<grid_for(C.n), 256, 0, s>>>(C.e_f, C.e, C.n);
+    NB_CUDA(cudaGetLastError());
+  }
+  for (int l = 2; l <= Lm - 1; ++l)
+    NB_TRY(mg_intp_add<T>(mg, V::e(mg.lv[l]), V::e(mg.lv[l - 1]), l - 1, s));
+  return mg_intp_add<T>(mg, zT, V::e(mg.lv[Lm - 1]), Lm - 1, s);
 }
 
 }  // namespace
 
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s) {
-  const int Lm = mg.nlev;
-  MgLevel &T = mg.lv[Lm];
-  NB_TRY(mg_schwarz(mg, z, rhs, Lm, s));
-  NB_TRY(vec_copy<double>(T.r, rhs, T.n, s));
-  for (int l = Lm - 1; l >= 2; --l) {
-    NB_TRY(mg_rstr(mg, mg.lv[l].r, mg.lv[l + 1].r, l, true, s));
-    NB_TRY(mg_schwarz(mg, mg.lv[l].e, mg.lv[l].r, l, s));
-  }
-  MgLevel &C = mg.lv[1];
-  NB_TRY(mg_rstr(mg, C.r, mg.lv[2].r, 1, false, s));
-  NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
-  NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));  // hsmg_coarse_solve
-  NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
-  NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
-  for (int l = 2; l <= Lm - 1; ++l) NB_TRY(mg_intp_add(mg, mg.lv[l].e, mg.lv[l - 1].e, l - 1, s));
-  return mg_intp_add(mg, z, mg.lv[Lm - 1].e, Lm - 1, s);
+  if (mg.precision == 64) return vcycle<double>(mg, z, rhs, s);
+  MgLevel &Top = mg.lv[mg.nlev];
+  // the reference masks rhs in place (h1mg_schwarz_part1, hsmg.f:1067)
+  NB_TRY(vec_mask<double>(rhs, Top.mask, Top.nmask, s));
+  k_to_f32<<<grid_for(Top.n), 256, 0, s>>>(Top.r_f, rhs, Top.n);
+  NB_CUDA(cudaGetLastError());
+  NB_TRY(vcycle<float>(mg, mg.z_f, Top.r_f, s));
+  k_to_f64<<<grid_for(Top.n), 256, 0, s>>>(z, mg.z_f, Top.n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
 }
 
 }  // namespace nb

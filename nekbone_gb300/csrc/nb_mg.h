@@ -20,6 +20,10 @@ struct MgLevel {
   int nmask = 0;
   double *jh = nullptr, *jht = nullptr;  // to the next finer level (nf x nc)
   double *e = nullptr, *r = nullptr;     // level vectors
+  // FP32 copies for the FP32 smoother
+  float *rstr_wt_f = nullptr, *fast_s_f = nullptr, *fast_d_f = nullptr,
+        *schwarz_wt_f = nullptr, *jh_f = nullptr, *jht_f = nullptr, *e_f = nullptr,
+        *r_f = nullptr;
 };
 
 struct Multigrid {
@@ -28,6 +32,8 @@ struct Multigrid {
   MgLevel lv[8];                  // 1-based
   double *A = nullptr, *B = nullptr;  // extended work arrays (finest size)
   double *w = nullptr;            // interpolation result
+  int precision = 64;             // 64, or 32: FP32 Schwarz smoother and transfers
+  float *A_f = nullptr, *B_f = nullptr, *z_f = nullptr;
   ~Multigrid();
 };
 
@@ -35,7 +41,7 @@ struct Multigrid {
 // choice (h1mg_setup_mg_nx, hsmg.f:45-97; defined only for lx1 <= 10);
 // otherwise nlev polynomial orders, coarsest first, the last = lx1-1.
 int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
-             cudaStream_t s);
+             cudaStream_t s, int precision = 64);
 // h1mg_solve (hsmg.f:960-1034): z = M^-1 rhs; masks rhs in place.
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s);
 

@@ -612,6 +612,12 @@ int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
                             false, s);
 }
 
+int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
+                const double *c, double *r, double *w, double *p, double *z,
+                int it0, int it1, Precond *M, cudaStream_t s) {
+  return cg_steps_t<double>(op, wk, x, g, c, r, w, p, z, it0, it1, -1, M, false, s);
+}
+
 int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
                   const float *g, const float *c, float *r, float *w, float *p,
                   int niter, cudaStream_t s) {

@@ -132,6 +132,10 @@ int launch_gs_fin(const Operator &op, CgWork &wk, double *w, const double *p,
 int launch_cg_update(const Operator &op, CgWork &wk, double *x, double *r,
                      const double *p, const double *w, const double *c,
                      int iter, cudaStream_t s);
+// iterations it0..it1 with preconditioner M (z = M^-1 r), scalars on device
+int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
+                const double *c, double *r, double *w, double *p, double *z,
+                int it0, int it1, Precond *M, cudaStream_t s);
 // FP32 variant (inner solves of the mixed-precision path), x starts at 0.
 int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
                   const float *g, const float *c, float *r, float *w, float *p,
