@@ -59,6 +59,8 @@ def test_deformed_metric_is_spd_and_operator_symmetric(torch):
     rng = np.random.default_rng(3)
     u = rng.standard_normal(glo.max() + 1)[glo]
     v = rng.standard_normal(glo.max() + 1)[glo]
+    ctx.maskit(u)   # the masked operator is symmetric on masked vectors
+    ctx.maskit(v)
     gh = np.ascontiguousarray(g.cpu().numpy())
     au, av = ctx.ax(u, gh), ctx.ax(v, gh)
     L = O.load()
