@@ -231,6 +231,11 @@ int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
                const double *c, double tol, int max_iter, int check_every,
                int *iters, double *relres);
 
+/* Self-test of the tensor-core (tcgen05) building blocks: one 128x16x16
+ * MMA of small integers (bf16 != 0: BF16 operands, else F16) compared with
+ * the exact product; *mismatches = number of wrong results (0 = pass). */
+int nb_tc_selftest(int bf16, int *mismatches);
+
 /* Synchronise the library's stream. */
 int nb_sync(void);
 /* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for

@@ -41,7 +41,7 @@ EXPORTS = (
     "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
     "nekbone_get_flops_", "nekbone_set_flops_", "nekbone_set_contraction_order_",
     "nb_mesh_set_order", "nb_setup_g_deformed", "nb_ax_f32", "nb_mg_setup",
-    "nb_mg_solve", "nb_pcg_tol", "gs_setup_", "gs_op_",
+    "nb_mg_solve", "nb_pcg_tol", "nb_tc_selftest", "gs_setup_", "gs_op_",
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
@@ -61,6 +61,8 @@ for _name in ("nb_mesh_create", "nb_mesh_destroy", "nb_mesh_info", "nb_setup_g",
               "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync"):
     getattr(lib, _name).restype = _i
 lib.nb_mesh_npts.argtypes = [_p]
+lib.nb_tc_selftest.restype = _i
+lib.nb_tc_selftest.argtypes = [_i, _p]
 lib.nb_mg_setup.restype = _i
 lib.nb_mg_setup.argtypes = [_p, _p, _i, _i]
 lib.nb_mg_solve.restype = _i
@@ -447,6 +449,13 @@ class DeviceMesh:
         _check(lib.nb_cg_tol(self._h, _p(x), _p(f), _p(g), _p(c), tol, max_iter,
                              check_every, _C.byref(it), _C.byref(rr)))
         return it.value, rr.value
+
+
+def tc_selftest(bf16: bool = False) -> int:
+    """Runs one tcgen05 MMA on known operands; returns the mismatch count."""
+    bad = _C.c_int(-1)
+    _check(lib.nb_tc_selftest(1 if bf16 else 0, _C.byref(bad)))
+    return bad.value
 
 
 def stream_handle() -> int:
