@@ -171,11 +171,27 @@ def run_reference(a, rank, world):
 
 
 # ---------------------------------------------------------------- extras --
+def _time_on(stream, torch, fn, reps=10):
+    """Average milliseconds of fn() over reps calls, CUDA events on stream."""
+    fn()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def extras(nb, torch, dev):
-    """Deformed-geometry operator error per lx1 (16^3 elements) and
-    hsmg-preconditioned CG against plain CG (16^3 deformed, lx1=12,
-    levels 12 -> 6 -> 3), to relative residual 1e-10."""
+    """Deformed-geometry operator error per lx1 (16^3 elements) for the
+    CUDA-core FP32 and the tensor-core (FP16 hi+lo split) operators, with
+    each operator's time, and hsmg-preconditioned CG against plain CG (16^3
+    deformed, lx1=12, levels 12 -> 6 -> 3), to relative residual 1e-10."""
     res = {"deformed_operator_error": {}, "hsmg_pcg": {}}
+    stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
     for lx in (8, 12, 16):
         m = nb.DeviceMesh(16, 16, 16, lx, mask_mode=1)
         n = m.n
@@ -190,10 +206,22 @@ def extras(nb, torch, dev):
         w32 = torch.empty(n, dtype=torch.float32, device=dev)
         u32, g32 = u.float(), g.float()
         m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())
+        wtc = torch.empty(n, dtype=torch.float32, device=dev)
+        m.ax_tc(wtc.data_ptr(), u32.data_ptr(), g32.data_ptr())
         torch.cuda.synchronize()
-        d = (w32.double() - w64).abs().max().item() / w64.abs().max().item()
-        res["deformed_operator_error"][f"lx1={lx}"] = {"fp32": d, "n": n}
-        del g, u, w64, w32, u32, g32
+        sc = w64.abs().max().item()
+        d = (w32.double() - w64).abs().max().item() / sc
+        dtc = (wtc.double() - w64).abs().max().item() / sc
+        ms = {
+            "fp64": _time_on(stream, torch, lambda: m.ax(w64.data_ptr(), u.data_ptr(), g.data_ptr())),
+            "fp32": _time_on(stream, torch,
+                             lambda: m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())),
+            "tc": _time_on(stream, torch,
+                           lambda: m.ax_tc(wtc.data_ptr(), u32.data_ptr(), g32.data_ptr())),
+        }
+        res["deformed_operator_error"][f"lx1={lx}"] = {"fp32": d, "tc": dtc, "n": n,
+                                                       "apply_ms": ms}
+        del g, u, w64, w32, u32, g32, wtc
         m.close()
         torch.cuda.empty_cache()
     m = nb.DeviceMesh(16, 16, 16, 12, mask_mode=1)

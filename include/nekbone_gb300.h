@@ -171,6 +171,11 @@ int nb_rhs_uniform(nb_mesh *mesh, double *f, const double *c, uint64_t seed);
 int nb_ax(nb_mesh *mesh, double *w, const double *u, const double *g);
 /* w = A u with the FP32 operator (FP32 u, w and g of 6n floats) */
 int nb_ax_f32(nb_mesh *mesh, float *w, const float *u, const float *g);
+/* The same with the six derivative contractions on the tcgen05 tensor
+ * cores: lines of each element as rows of K-major FP16 tiles, scaled to unit
+ * maximum and split hi + lo, three MMAs per tile (hi*hi + hi*lo + lo*hi)
+ * accumulated in FP32; metric and sums in FP32 on CUDA cores. */
+int nb_ax_tc(nb_mesh *mesh, float *w, const float *u, const float *g);
 /* dssum on a device vector (dom 1 double, 2 float) */
 int nb_dssum(nb_mesh *mesh, void *u, int dom);
 

@@ -41,7 +41,7 @@ EXPORTS = (
     "nekbone_mask_reset_", "nekbone_set_mask_mode_", "nekbone_set_mgrid_",
     "nekbone_get_flops_", "nekbone_set_flops_", "nekbone_set_contraction_order_",
     "nb_mesh_set_order", "nb_setup_g_deformed", "nb_ax_f32", "nb_mg_setup",
-    "nb_mg_solve", "nb_pcg_tol", "nb_tc_selftest", "gs_setup_", "gs_op_",
+    "nb_mg_solve", "nb_pcg_tol", "nb_tc_selftest", "nb_ax_tc", "gs_setup_", "gs_op_",
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
@@ -71,6 +71,8 @@ lib.nb_pcg_tol.restype = _i
 lib.nb_pcg_tol.argtypes = [_p, _p, _p, _p, _p, _d, _i, _i, _p, _p]
 lib.nb_setup_g_deformed.restype = _i
 lib.nb_setup_g_deformed.argtypes = [_p, _p, _C.c_uint64, _d]
+lib.nb_ax_tc.restype = _i
+lib.nb_ax_tc.argtypes = [_p, _p, _p, _p]
 lib.nb_ax_f32.restype = _i
 lib.nb_ax_f32.argtypes = [_p, _p, _p, _p]
 lib.nb_mesh_set_order.restype = _i
@@ -382,6 +384,9 @@ class DeviceMesh:
 
     def setup_g_deformed(self, g_ptr: int, seed: int, amp: float = 0.1) -> None:
         _check(lib.nb_setup_g_deformed(self._h, _p(g_ptr), seed, amp))
+
+    def ax_tc(self, w_ptr: int, u_ptr: int, g_ptr: int) -> None:
+        _check(lib.nb_ax_tc(self._h, _p(w_ptr), _p(u_ptr), _p(g_ptr)))
 
     def ax_f32(self, w_ptr: int, u_ptr: int, g_ptr: int) -> None:
         _check(lib.nb_ax_f32(self._h, _p(w_ptr), _p(u_ptr), _p(g_ptr)))

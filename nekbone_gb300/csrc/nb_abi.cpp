@@ -35,6 +35,7 @@ int dev_rhs_uniform(const Operator &op, double *f, const double *c,
                     uint64_t seed, cudaStream_t s);
 int dev_setup_g_deformed(const Operator &op, double *g, uint64_t seed, double amp,
                          cudaStream_t s);
+int apply_ax_tc(const Operator &op, float *w, const float *u, const float *g, cudaStream_t s);
 int dev_residual(const Operator &op, double *r, const double *f,
                  const double *w, long n, cudaStream_t s);
 int dev_axpy_f32(double *x, const float *e, double scale, long n, cudaStream_t s);
@@ -741,6 +742,14 @@ int nb_setup_g_deformed(nb_mesh *mesh, double *g, uint64_t seed, double amp) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
   return dev_setup_g_deformed(mesh->op, g, seed, amp, st().s);
+}
+
+int nb_ax_tc(nb_mesh *mesh, float *w, const float *u, const float *g) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (mesh->op.mask_mode == 0 && !mesh->op.mask_built)
+    return fail(NB_ERR_STATE, "nb_ax_tc: the reference mask list is not built yet");
+  return apply_ax_tc(mesh->op, w, u, g, st().s);
 }
 
 int nb_ax_f32(nb_mesh *mesh, float *w, const float *u, const float *g) {

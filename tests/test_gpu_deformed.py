@@ -98,3 +98,33 @@ def test_fp32_operator_error_vs_fp64_oracle(torch, lx):
     err = np.max(np.abs(w32.cpu().numpy().astype(np.float64) - w64)) / np.max(np.abs(w64))
     print(f"lx1={lx}: FP32 operator max rel error vs FP64 oracle {err:.3e}")
     assert err < 2e-5
+
+
+@pytest.mark.parametrize("lx", [4, 8, 10, 12, 16])
+def test_tensor_core_operator_error_vs_fp64_oracle(torch, lx):
+    """tcgen05 FP16 hi+lo split contractions with FP32 accumulation: the
+    operator agrees with the FP64 oracle to FP32 accuracy (2e-5 relative,
+    the same bound as the CUDA-core FP32 operator)."""
+    import nekbone_gb300 as nb
+    nel = 4 if lx <= 12 else 3
+    m, g = _mesh_and_g(nb, torch, nel, lx, seed=5)
+    ctx = O.Ctx(nel, nel, nel, lx, mask_mode=1)
+    glo = O.set_vert_box(lx, ctx.nelt, nel, nel, nel, ctx.lglel)
+    rng = np.random.default_rng(100 + lx)
+    u = rng.uniform(-1, 1, glo.max() + 1)[glo]
+    gh = np.ascontiguousarray(g.cpu().numpy())
+    w64 = ctx.ax(u, gh)
+    ut = torch.from_numpy(u).cuda().float()
+    g32 = g.float()
+    wt = torch.full((m.n,), float("nan"), dtype=torch.float32, device="cuda")
+    m.ax_tc(wt.data_ptr(), ut.data_ptr(), g32.data_ptr())
+    w32 = torch.empty(m.n, dtype=torch.float32, device="cuda")
+    m.ax_f32(w32.data_ptr(), ut.data_ptr(), g32.data_ptr())
+    torch.cuda.synchronize()
+    got = wt.cpu().numpy().astype(np.float64)
+    assert np.all(np.isfinite(got))
+    scale = np.max(np.abs(w64))
+    err_tc = np.max(np.abs(got - w64)) / scale
+    err_f32 = np.max(np.abs(w32.cpu().numpy().astype(np.float64) - w64)) / scale
+    print(f"lx1={lx}: tensor-core operator max rel error {err_tc:.3e} (CUDA-core FP32 {err_f32:.3e})")
+    assert err_tc < 2e-5
