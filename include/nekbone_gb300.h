@@ -260,6 +260,48 @@ int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
                            const float *g, const float *c, float *r, float *w,
                            float *p, int reps, double *ms3);
 
+/* ------------------------------------------- batched solves (nb_batch_*) --
+ * Many independent box-mesh Dirichlet Poisson problems of uneven element
+ * counts and orders (lx1 in {4, 6, 8, 10, 12}), solved together by the
+ * mixed solver (FP32 inner CG inside FP64 defect correction) as one CUDA
+ * graph launch.  No counterpart in the reference, which solves one mesh per
+ * process (driver.f:42-59); each problem is the mesh nb_mesh_create builds
+ * with mask_mode 1, and its vectors live at nb_batch_problem's offset in the
+ * batch's concatenated device arrays. */
+typedef struct nb_batch nb_batch;
+int nb_batch_create(nb_batch **batch, int nprob, const int *nelx, const int *nely,
+                    const int *nelz, const int *lx1);
+int nb_batch_destroy(nb_batch *batch);
+/* total points, total elements, number of distinct lx1 */
+int nb_batch_info(const nb_batch *batch, long *npts, int *nelt, int *nlx);
+int nb_batch_problem(const nb_batch *batch, int prob, long *pt_offset, long *npts,
+                     int *lx1);
+/* device pointers of the concatenated x, f, c (n each) and g (6n) */
+int nb_batch_arrays(nb_batch *batch, double **x, double **f, double **g, double **c);
+/* g = setup_g form, c = inverse multiplicity, f of problem p = the
+ * nb_rhs_uniform right-hand side with seed + p */
+int nb_batch_setup(nb_batch *batch, uint64_t seed);
+/* Autotuner: times every instantiated shape (elements per block, D in
+ * registers or shared memory) of the FP32 inner and FP64 defect element
+ * operators on the batch's elements of each lx1, reps launches each, and
+ * keeps the fastest.  Overwrites x. */
+int nb_batch_tune(nb_batch *batch, int reps);
+int nb_batch_get_tuning(const nb_batch *batch, int lx1, int *epb32, int *rd32, int *epb64,
+                        float *ms32, float *ms64);
+int nb_batch_set_tuning(nb_batch *batch, int lx1, int epb32, int rd32, int epb64);
+/* Enqueues the solve of every problem to |r|_C / |f|_C <= tol (cycles of
+ * inner_iters FP32 CG iterations, at most max_outer cycles) as one graph
+ * launch on the library stream; x starts at 0. */
+int nb_batch_solve(nb_batch *batch, double tol, int inner_iters, int max_outer);
+/* per problem: cycles, inner iterations, final |r|_C / |f|_C (synchronises) */
+int nb_batch_result(const nb_batch *batch, int prob, int *outer, int *inner, double *relres);
+/* cycles the last solve's loop ran */
+int nb_batch_cycles(const nb_batch *batch, int *cycles);
+/* asynchronous copies of the whole concatenated f in / x out (pinned host
+ * buffers of nb_batch_info's npts doubles) */
+int nb_batch_rhs_in(nb_batch *batch, const double *f_host);
+int nb_batch_x_out(nb_batch *batch, double *x_host);
+
 #ifdef __cplusplus
 }
 #endif

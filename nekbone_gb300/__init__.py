@@ -50,6 +50,10 @@ EXPORTS = (
     "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
     "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync", "nb_stream",
     "nb_time_cg_kernels", "nb_glsc3_noalloc", "nb_time_cg_kernels_f32",
+    "nb_batch_create", "nb_batch_destroy", "nb_batch_info", "nb_batch_problem",
+    "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
+    "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
+    "nb_batch_rhs_in", "nb_batch_x_out",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -95,6 +99,23 @@ lib.nb_time_cg_kernels_f32.restype = _i
 lib.nb_time_cg_kernels_f32.argtypes = [_p, _p, _p, _p, _p, _p, _p, _p, _i, _p]
 lib.nb_glsc3_noalloc.restype = _i
 lib.nb_glsc3_noalloc.argtypes = [_p, _p, _p, _l, _p, _p]
+for _name, _args in (
+        ("nb_batch_create", [_p, _i, _p, _p, _p, _p]),
+        ("nb_batch_destroy", [_p]),
+        ("nb_batch_info", [_p, _p, _p, _p]),
+        ("nb_batch_problem", [_p, _i, _p, _p, _p]),
+        ("nb_batch_arrays", [_p, _p, _p, _p, _p]),
+        ("nb_batch_setup", [_p, _C.c_uint64]),
+        ("nb_batch_tune", [_p, _i]),
+        ("nb_batch_get_tuning", [_p, _i, _p, _p, _p, _p, _p]),
+        ("nb_batch_set_tuning", [_p, _i, _i, _i, _i]),
+        ("nb_batch_solve", [_p, _d, _i, _i]),
+        ("nb_batch_result", [_p, _i, _p, _p, _p]),
+        ("nb_batch_cycles", [_p, _p]),
+        ("nb_batch_rhs_in", [_p, _p]),
+        ("nb_batch_x_out", [_p, _p])):
+    getattr(lib, _name).restype = _i
+    getattr(lib, _name).argtypes = _args
 #: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
 NOALLOC_MAX_N = 67108864
 
@@ -454,6 +475,87 @@ class DeviceMesh:
         _check(lib.nb_cg_tol(self._h, _p(x), _p(f), _p(g), _p(c), tol, max_iter,
                              check_every, _C.byref(it), _C.byref(rr)))
         return it.value, rr.value
+
+
+class Batch:
+    """Many independent box-mesh problems solved together (nb_batch_*).
+
+    ``boxes`` is a sequence of (nelx, nely, nelz, lx1).  Device vectors of
+    problem p live at ``offset(p)`` in the concatenated arrays whose device
+    pointers ``arrays()`` returns."""
+
+    def __init__(self, boxes):
+        boxes = [tuple(int(v) for v in b) for b in boxes]
+        self.nprob = len(boxes)
+        col = [_np.ascontiguousarray([b[k] for b in boxes], dtype=_np.int32) for k in range(4)]
+        h = _C.c_void_p()
+        _check(lib.nb_batch_create(_C.byref(h), self.nprob, *[_ptr(c) for c in col]))
+        self._h = h
+        self.boxes = boxes
+        n, ne, nl = _C.c_long(), _C.c_int(), _C.c_int()
+        _check(lib.nb_batch_info(self._h, _C.byref(n), _C.byref(ne), _C.byref(nl)))
+        self.n, self.nelt, self.nlx = n.value, ne.value, nl.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib.nb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def problem(self, p: int):
+        """(point offset, number of points, lx1) of problem p"""
+        o, n, l = _C.c_long(), _C.c_long(), _C.c_int()
+        _check(lib.nb_batch_problem(self._h, p, _C.byref(o), _C.byref(n), _C.byref(l)))
+        return o.value, n.value, l.value
+
+    def arrays(self):
+        """device pointers (x, f, g, c)"""
+        ptrs = [_C.c_void_p() for _ in range(4)]
+        _check(lib.nb_batch_arrays(self._h, *[_C.byref(q) for q in ptrs]))
+        return tuple(q.value for q in ptrs)
+
+    def setup(self, seed: int) -> None:
+        _check(lib.nb_batch_setup(self._h, _C.c_uint64(seed)))
+
+    def tune(self, reps: int = 3) -> None:
+        _check(lib.nb_batch_tune(self._h, reps))
+
+    def tuning(self, lx: int):
+        e32, r32, e64 = _C.c_int(), _C.c_int(), _C.c_int()
+        m32, m64 = _C.c_float(), _C.c_float()
+        _check(lib.nb_batch_get_tuning(self._h, lx, _C.byref(e32), _C.byref(r32), _C.byref(e64),
+                                       _C.byref(m32), _C.byref(m64)))
+        return {"epb32": e32.value, "rd32": r32.value, "epb64": e64.value,
+                "ms32": m32.value, "ms64": m64.value}
+
+    def set_tuning(self, lx: int, epb32: int, rd32: int, epb64: int) -> None:
+        _check(lib.nb_batch_set_tuning(self._h, lx, epb32, rd32, epb64))
+
+    def solve(self, tol: float = 1e-10, inner_iters: int = 20, max_outer: int = 50) -> None:
+        """enqueue the whole solve (one graph launch) on the library stream"""
+        _check(lib.nb_batch_solve(self._h, _C.c_double(tol), inner_iters, max_outer))
+
+    def result(self, p: int):
+        """(cycles, inner iterations, |r|_C/|f|_C) of problem p"""
+        o, i, rr = _C.c_int(), _C.c_int(), _C.c_double()
+        _check(lib.nb_batch_result(self._h, p, _C.byref(o), _C.byref(i), _C.byref(rr)))
+        return o.value, i.value, rr.value
+
+    def cycles(self) -> int:
+        v = _C.c_int()
+        _check(lib.nb_batch_cycles(self._h, _C.byref(v)))
+        return v.value
+
+    def rhs_in(self, host_ptr: int) -> None:
+        _check(lib.nb_batch_rhs_in(self._h, _C.c_void_p(host_ptr)))
+
+    def x_out(self, host_ptr: int) -> None:
+        _check(lib.nb_batch_x_out(self._h, _C.c_void_p(host_ptr)))
 
 
 def tc_selftest(bf16: bool = False) -> int:

@@ -1,0 +1,1118 @@
+// nb_batch.cu -- many independent box-mesh Poisson problems solved together.
+//
+// Every problem is a brick of nelx*nely*nelz elements with its own lx1, the
+// reference's numbering (set_vert_box, prox_dssum.f:42-73), the undeformed
+// metric (setup_g, prox_setup.f:27-52), the full Dirichlet mask and a
+// seeded uniform right-hand side.  The solver is the mixed one of a single
+// mesh -- FP32 inner CG (cg.f:48-75 with z = r, fixed inner iterations)
+// inside FP64 defect correction to |r|_C / |f|_C <= tol -- run for all
+// problems at once:
+//
+//   * all problems' points, elements and element-boundary groups are
+//     concatenated, problems ordered by lx1 so that each lx1 is one element
+//     range (one launch of the batched element operator per lx1);
+//   * the gather-scatter, vector and norm kernels work on chunks that never
+//     straddle a problem; each chunk writes one partial, and the chunk that
+//     arrives last for its problem (a per-problem counter) sums that
+//     problem's partials in a fixed order, so every per-problem scalar is
+//     deterministic;
+//   * converged problems drop out (every kernel skips their chunks);
+//   * the whole solve -- initial norms, then cycles of [scale, inner CG,
+//     FP64 defect, convergence test] -- is one CUDA graph: the cycle is the
+//     body of a conditional WHILE node whose condition a one-block kernel
+//     sets from the problems' active flags (and a cycle bound), so a single
+//     graph launch runs the solve to the end with no host round trip.
+//
+// The shape of the element operator per lx1 (elements per block and the D
+// operand form) is chosen by nb_batch_tune, which times every instantiated
+// shape on the batch's own elements.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+#include "../../include/nekbone_gb300.h"
+#include "nb_batch.h"
+
+namespace nb {
+
+cudaStream_t lib_stream();
+
+namespace {
+
+constexpr int kGroupChunk = 256;   // boundary groups per chunk, one per thread
+constexpr int kPointChunk = 2048;  // points per chunk, eight per thread
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------- kernels --
+// Boundary groups of the inner FP32 iteration (k_gs_fin per problem): w =
+// jl-order group sum of w_L + 0.1 p (0 when masked), the boundary part of
+// pap; the problem's last chunk forms pap and alpha = rtz1 / pap.
+__global__ void __launch_bounds__(kThreads)
+    k_bgs_fin(float *__restrict__ w, const float *__restrict__ p, const float *__restrict__ c,
+              const int *__restrict__ off, const unsigned *__restrict__ idx,
+              const int *__restrict__ gch_g0, const int *__restrict__ gch_prob,
+              const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_gs,
+              const double *__restrict__ part_ax, unsigned *cnt) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x;
+  const int prob = gch_prob[ch];
+  if (!sc[prob].active) return;
+  const int g = gch_g0[ch] + threadIdx.x;
+  float part = 0.f;
+  if (g < gch_g0[ch + 1]) {
+    const int b = off[g], e = off[g + 1];
+    float t = w[idx[b] & 0x7fffffffu];
+    for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
+    unsigned mm[8];
+    float pv[8], cv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < e - b) {
+        mm[q] = idx[b + q];
+        pv[q] = p[mm[q] & 0x7fffffffu];
+        cv[q] = c[mm[q] & 0x7fffffffu];
+      }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < e - b) {
+        float v = fma_rn(0.1f, pv[q], t);
+        if (mm[q] & 0x80000000u) v = 0.f;
+        w[mm[q] & 0x7fffffffu] = v;
+        part = fma_rn(mul_rn(v, cv[q]), pv[q], part);
+      }
+  }
+  const double s = block_sum<float>(part, red);
+  if (threadIdx.x == 0) part_gs[ch] = s;
+  const BatchProb P = pb[prob];
+  if (last_block(cnt + prob, P.ngc)) {
+    const double s1 = block_sum_array(part_ax + P.el0, P.nelt, red);
+    __syncthreads();
+    const double s2 = block_sum_array(part_gs + P.gc0, P.ngc, red);
+    if (threadIdx.x == 0) {
+      const double pap = s1 + s2;
+      sc[prob].pap = pap;
+      sc[prob].alpha = pap != 0.0 ? sc[prob].rtz1 / pap : 0.0;
+    }
+  }
+}
+
+// Boundary groups of the FP64 defect: A x = group sum + 0.1 x (0 when
+// masked), r = f - A x, boundary part of r'Cr; the problem's last chunk
+// forms |r|_C, counts the cycle and decides whether the problem goes on.
+__global__ void __launch_bounds__(kThreads)
+    k_bgs_res(const double *__restrict__ w, const double *__restrict__ x,
+              const double *__restrict__ f, double *__restrict__ r, const double *__restrict__ c,
+              const int *__restrict__ off, const unsigned *__restrict__ idx,
+              const int *__restrict__ gch_g0, const int *__restrict__ gch_prob,
+              const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_gs,
+              const double *__restrict__ part_ax, unsigned *cnt, double tol, int inner_iters,
+              int max_outer) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x;
+  const int prob = gch_prob[ch];
+  if (!sc[prob].active) return;
+  const int g = gch_g0[ch] + threadIdx.x;
+  double part = 0.0;
+  if (g < gch_g0[ch + 1]) {
+    const int b = off[g], e = off[g + 1];
+    double t = w[idx[b] & 0x7fffffffu];
+    for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
+    unsigned mm[8];
+    double xv[8], fv[8], cv[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < e - b) {
+        mm[q] = idx[b + q];
+        const unsigned id = mm[q] & 0x7fffffffu;
+        xv[q] = x[id];
+        fv[q] = f[id];
+        cv[q] = c[id];
+      }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (q < e - b) {
+        double ax = fma_rn(0.1, xv[q], t);
+        if (mm[q] & 0x80000000u) ax = 0.0;
+        const double rv = fv[q] - ax;
+        r[mm[q] & 0x7fffffffu] = rv;
+        part = fma_rn(mul_rn(rv, cv[q]), rv, part);
+      }
+  }
+  const double s = block_sum<double>(part, red);
+  if (threadIdx.x == 0) part_gs[ch] = s;
+  const BatchProb P = pb[prob];
+  if (last_block(cnt + prob, P.ngc)) {
+    const double s1 = block_sum_array(part_ax + P.el0, P.nelt, red);
+    __syncthreads();
+    const double s2 = block_sum_array(part_gs + P.gc0, P.ngc, red);
+    if (threadIdx.x == 0) {
+      BatchScalars &S = sc[prob];
+      S.rtr = s1 + s2;
+      S.rn = sqrt(s1 + s2);
+      S.outer += 1;
+      S.inner += inner_iters;
+      const bool converged = S.rn <= tol * S.rn0;
+      S.active = (!converged && S.outer < max_outer) ? 1 : 0;
+    }
+  }
+}
+
+// Inner FP32 update (k_cg_update per problem): x += alpha p, r -= alpha w,
+// r'Cr; the problem's last chunk forms rtz1 and beta (z = r).
+__global__ void __launch_bounds__(kThreads)
+    k_bupd(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
+           const float *__restrict__ w, const float *__restrict__ c,
+           const long *__restrict__ pch_q0, const int *__restrict__ pch_prob,
+           const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_pt,
+           unsigned *cnt) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x;
+  const int prob = pch_prob[ch];
+  if (!sc[prob].active) return;
+  const float alpha = float(sc[prob].alpha);
+  const float alphm = -alpha;
+  const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
+  float part = 0.f;
+#pragma unroll 4
+  for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
+    const float pv = p[q], wv = w[q], rv0 = r[q], xv = x[q], cv = c[q];
+    x[q] = fma_rn(alpha, pv, xv);
+    const float rv = fma_rn(alphm, wv, rv0);
+    r[q] = rv;
+    part = fma_rn(mul_rn(rv, cv), rv, part);
+  }
+  const double s = block_sum<float>(part, red);
+  if (threadIdx.x == 0) part_pt[ch] = s;
+  const BatchProb P = pb[prob];
+  if (last_block(cnt + prob, P.npc)) {
+    const double rtr = block_sum_array(part_pt + P.pc0, P.npc, red);
+    if (threadIdx.x == 0) {
+      BatchScalars &S = sc[prob];
+      S.rtr = rtr;
+      S.rtz2 = S.rtz1;
+      S.rtz1 = rtr;
+      S.beta = S.rtz2 != 0.0 ? S.rtz1 / S.rtz2 : 0.0;
+    }
+  }
+}
+
+// Start of a cycle: inner right-hand side r32 = r / |r|, inner x = 0, and
+// the inner rtz1 = r32'C r32.
+__global__ void __launch_bounds__(kThreads)
+    k_bscale(float *__restrict__ r32, float *__restrict__ e32, const double *__restrict__ r,
+             const float *__restrict__ c32, const long *__restrict__ pch_q0,
+             const int *__restrict__ pch_prob, const BatchProb *__restrict__ pb,
+             BatchScalars *sc, double *__restrict__ part_pt, unsigned *cnt) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x;
+  const int prob = pch_prob[ch];
+  if (!sc[prob].active) return;
+  const double inv = 1.0 / sc[prob].rn;
+  const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
+  float part = 0.f;
+#pragma unroll 4
+  for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
+    const float v = float(r[q] * inv);
+    r32[q] = v;
+    e32[q] = 0.f;
+    part = fma_rn(mul_rn(v, c32[q]), v, part);
+  }
+  const double s = block_sum<float>(part, red);
+  if (threadIdx.x == 0) part_pt[ch] = s;
+  const BatchProb P = pb[prob];
+  if (last_block(cnt + prob, P.npc)) {
+    const double rtz = block_sum_array(part_pt + P.pc0, P.npc, red);
+    if (threadIdx.x == 0) {
+      sc[prob].rtz1 = rtz;
+      sc[prob].beta = 0.0;
+    }
+  }
+}
+
+// Initial state: x = 0, r = f, |f|_C; a problem with f = 0 (or no cycles
+// allowed) is inactive from the start.
+__global__ void __launch_bounds__(kThreads)
+    k_binit(double *__restrict__ x, double *__restrict__ r, const double *__restrict__ f,
+            const double *__restrict__ c, const long *__restrict__ pch_q0,
+            const int *__restrict__ pch_prob, const BatchProb *__restrict__ pb,
+            BatchScalars *sc, double *__restrict__ part_pt, unsigned *cnt, int max_outer) {
+  __shared__ double red[32];
+  const int ch = blockIdx.x;
+  const int prob = pch_prob[ch];
+  const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
+  double part = 0.0;
+  for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
+    const double fv = f[q];
+    x[q] = 0.0;
+    r[q] = fv;
+    part = fma_rn(mul_rn(fv, c[q]), fv, part);
+  }
+  const double s = block_sum<double>(part, red);
+  if (threadIdx.x == 0) part_pt[ch] = s;
+  const BatchProb P = pb[prob];
+  if (last_block(cnt + prob, P.npc)) {
+    const double ff = block_sum_array(part_pt + P.pc0, P.npc, red);
+    if (threadIdx.x == 0) {
+      BatchScalars &S = sc[prob];
+      S.rn0 = sqrt(ff);
+      S.rn = S.rn0;
+      S.rtr = ff;
+      S.outer = 0;
+      S.inner = 0;
+      S.active = (S.rn0 > 0.0 && max_outer > 0) ? 1 : 0;
+    }
+  }
+}
+
+// The loop condition: some problem still active and fewer than max_cycles
+// cycles run (a bound that holds whatever the per-problem tests do).
+__global__ void __launch_bounds__(kThreads)
+    k_bcontrol(const BatchScalars *sc, int nprob, int *cycles, int reset, int max_cycles,
+               cudaGraphConditionalHandle h) {
+  int any = 0;
+  for (int p = threadIdx.x; p < nprob; p += blockDim.x) any |= sc[p].active;
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) {
+    const int cyc = reset ? 0 : *cycles + 1;
+    *cycles = cyc;
+    cudaGraphSetConditional(h, (any && cyc < max_cycles) ? 1u : 0u);
+  }
+}
+
+// ---------------------------------------------------------- set-up kernels --
+// setup_g (prox_setup.f:27-52) on one lx1 range
+__global__ void k_bsetup_g(double *g, const double *wgt, int lx, long n) {
+  const long l3 = long(lx) * lx * lx;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    const int rr = int(q % l3);
+    const int i = rr % lx, j = (rr / lx) % lx, k = rr / (lx * lx);
+    const double v = wgt[i] * wgt[j] * wgt[k];
+    double *gp = g + 6 * q;
+    gp[0] = v;
+    gp[1] = 0.;
+    gp[2] = 0.;
+    gp[3] = v;
+    gp[4] = 0.;
+    gp[5] = v;
+  }
+}
+
+// uniform [-1,1) per global point of one problem (its box numbering)
+__global__ void k_brhs(double *f, int lx, int nelx, int nely, long n, uint64_t seed) {
+  const long l3 = long(lx) * lx * lx;
+  const int nn = lx - 1;
+  const long ax = long(nn) * nelx + 1, ay = long(nn) * nely + 1;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / l3;
+    const int rr = int(q % l3);
+    const int i = rr % lx, j = (rr / lx) % lx, k = rr / (lx * lx);
+    const long ex = e % nelx, ey = (e / nelx) % nely, ez = e / (long(nelx) * nely);
+    const long id = 1 + (nn * ex + i) + (nn * ey + j) * ax + (nn * ez + k) * ax * ay;
+    f[q] = uniform_pm1(seed, uint64_t(id));
+  }
+}
+
+// multiplicity: c = 1 / group size on boundary groups (interior points keep 1)
+__global__ void k_bmult(double *c, const int *off, const unsigned *idx, int ng) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    const double v = 1.0 / double(e - b);
+    for (int q = b; q < e; ++q) c[idx[q] & 0x7fffffffu] = v;
+  }
+}
+
+// set_f's dssum, col2(c), mask (driver.f:88-101) on boundary groups
+__global__ void k_bdssum_c_mask(double *f, const double *c, const int *off, const unsigned *idx,
+                                int ng) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    double t = f[idx[b] & 0x7fffffffu];
+    for (int q = b + 1; q < e; ++q) t = add_rn(t, f[idx[q] & 0x7fffffffu]);
+    for (int q = b; q < e; ++q) {
+      const unsigned m = idx[q], id = m & 0x7fffffffu;
+      f[id] = (m & 0x80000000u) ? 0.0 : mul_rn(t, c[id]);
+    }
+  }
+}
+
+__global__ void k_fill(double *a, double v, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = v;
+}
+
+template <typename T, typename S>
+__global__ void k_conv(T *a, const S *b, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = T(b[q]);
+}
+
+__global__ void k_set_active(BatchScalars *sc, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nprob) {
+    sc[p].active = 1;
+    sc[p].rn = 1.0;
+    sc[p].beta = 0.0;
+  }
+}
+
+int grid_for(long n) {
+  return int(std::max(1L, std::min<long>(152L * 8, (n + 255) / 256)));
+}
+
+// ------------------------------------------------------------- host set-up --
+bool elem_boundary(int r, int lx) {
+  const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+  return i == 0 || i == lx - 1 || j == 0 || j == lx - 1 || k == 0 || k == lx - 1;
+}
+
+// Element-boundary groups of one box problem in the order of the fused
+// single-mesh pass: groups of points with one global id (set_vert_box), in
+// ascending order of their first (smallest) local index, members ascending
+// -- jl's local map order (gs.c:88-113, 330-357) -- plus every unshared
+// boundary point as a group of one.  Members on a domain face carry bit 31.
+void box_groups(int nelx, int nely, int nelz, int lx, std::vector<int> &off,
+                std::vector<unsigned> &idx) {
+  const int nelt = nelx * nely * nelz;
+  const int l3 = lx * lx * lx;
+  const long n = long(nelt) * l3;
+  std::vector<int> lglel(nelt);
+  for (int e = 0; e < nelt; ++e) lglel[e] = e + 1;
+  std::vector<int64_t> glo(n);
+  set_vert_box(glo.data(), lx, nelt, nelx, nely, lglel.data());
+  std::vector<std::pair<int64_t, unsigned>> bp;
+  bp.reserve(size_t(nelt) * (l3 - (lx > 2 ? (lx - 2) * (lx - 2) * (lx - 2) : 0)));
+  for (long q = 0; q < n; ++q)
+    if (elem_boundary(int(q % l3), lx)) bp.push_back({glo[q], unsigned(q)});
+  std::sort(bp.begin(), bp.end());
+  // runs of equal id; order runs by first member
+  std::vector<std::pair<unsigned, std::pair<size_t, size_t>>> runs;
+  for (size_t a = 0; a < bp.size();) {
+    size_t b = a + 1;
+    while (b < bp.size() && bp[b].first == bp[a].first) ++b;
+    runs.push_back({bp[a].second, {a, b}});
+    a = b;
+  }
+  std::sort(runs.begin(), runs.end());
+  std::vector<unsigned char> face(nelt);
+  for (int e = 0; e < nelt; ++e) face[e] = (unsigned char)face_bits(e + 1, nelx, nely, nelz);
+  auto masked = [&](unsigned q) {
+    const unsigned f = face[q / l3];
+    if (!f) return false;
+    const int rr = int(q % l3);
+    const int i = rr % lx, j = (rr / lx) % lx, k = rr / (lx * lx);
+    return ((f & 1u) && i == 0) || ((f & 2u) && i == lx - 1) || ((f & 4u) && j == 0) ||
+           ((f & 8u) && j == lx - 1) || ((f & 16u) && k == 0) || ((f & 32u) && k == lx - 1);
+  };
+  off.clear();
+  idx.clear();
+  off.reserve(runs.size() + 1);
+  idx.reserve(bp.size());
+  for (const auto &rn : runs) {
+    off.push_back(int(idx.size()));
+    for (size_t q = rn.second.first; q < rn.second.second; ++q) {
+      const unsigned m = bp[q].second;
+      idx.push_back(m | (masked(m) ? 0x80000000u : 0u));
+    }
+  }
+  off.push_back(int(idx.size()));
+}
+
+}  // namespace
+
+// A batch of problems on the device.
+struct Batch {
+  struct Group {
+    int lx = 0, el0 = 0, nel = 0;
+    long pt0 = 0, n = 0;
+    double *D64 = nullptr;
+    float *D32 = nullptr;
+    BatchTune tune;
+  };
+  int nprob = 0;
+  std::vector<int> nelx, nely, nelz, lx;   // user order
+  std::vector<int> slot;                   // user index -> internal index
+  std::vector<BatchProb> P;                // internal order
+  std::vector<int> P_user;                 // internal index -> user index
+  std::vector<Group> groups;
+  long n = 0;
+  int nelt = 0, ng = 0, ngc = 0, npc = 0;
+  // device
+  double *x = nullptr, *f = nullptr, *g = nullptr, *c = nullptr, *r = nullptr, *w = nullptr;
+  float *g32 = nullptr, *c32 = nullptr, *r32 = nullptr, *e32 = nullptr, *p32 = nullptr,
+        *w32 = nullptr;
+  int *el_prob = nullptr, *off = nullptr, *gch_g0 = nullptr, *gch_prob = nullptr,
+      *pch_prob = nullptr, *cycles = nullptr;
+  unsigned *idx = nullptr, *cnt = nullptr;
+  long *pch_q0 = nullptr;
+  BatchProb *pb = nullptr;
+  BatchScalars *sc = nullptr;
+  double *part_ax = nullptr, *part_gs = nullptr, *part_pt = nullptr;
+  bool setup_done = false;
+  // the solve graph
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double g_tol = -1.0;
+  int g_inner = -1, g_outer = -1;
+
+  ~Batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (cap) cudaStreamDestroy(cap);
+    for (auto &G : groups) {
+      cudaFree(G.D64);
+      cudaFree(G.D32);
+    }
+    void *ptrs[] = {x, f, g, c, r, w, g32, c32, r32, e32, p32, w32, el_prob, off, gch_g0,
+                    gch_prob, pch_prob, cycles, idx, cnt, pch_q0, pb, sc, part_ax, part_gs,
+                    part_pt};
+    for (void *p : ptrs)
+      if (p) cudaFree(p);
+  }
+
+  int launch_inner_ax(int it, cudaStream_t s) const {
+    for (const auto &G : groups) {
+      BaxArgs<float> a{};
+      a.w = w32;
+      a.u = r32;
+      a.p = p32;
+      a.g = g32;
+      a.c = c32;
+      a.D = G.D32;
+      a.el_prob = el_prob;
+      a.sc = sc;
+      a.partial = part_ax;
+      a.pt0 = G.pt0;
+      a.el0 = G.el0;
+      a.nel = G.nel;
+      a.first = it == 1;
+      NB_TRY(batch_ax_f32(G.lx, G.tune.epb32, G.tune.rd32, a, s));
+    }
+    return NB_OK;
+  }
+  int launch_defect_ax(cudaStream_t s) const {
+    for (const auto &G : groups) {
+      BaxArgs<double> a{};
+      a.w = w;
+      a.p = x;
+      a.g = g;
+      a.c = c;
+      a.D = G.D64;
+      a.f = f;
+      a.r = r;
+      a.e = e32;
+      a.el_prob = el_prob;
+      a.sc = sc;
+      a.partial = part_ax;
+      a.pt0 = G.pt0;
+      a.el0 = G.el0;
+      a.nel = G.nel;
+      NB_TRY(batch_ax_f64(G.lx, G.tune.epb64, a, s));
+    }
+    return NB_OK;
+  }
+  static int batch_ax_f32(int lx, int epb, int rd, const BaxArgs<float> &a, cudaStream_t s) {
+    switch (lx) {
+      case 4: return batch_ax_f32_lx<4>(epb, rd, a, s);
+      case 6: return batch_ax_f32_lx<6>(epb, rd, a, s);
+      case 8: return batch_ax_f32_lx<8>(epb, rd, a, s);
+      case 10: return batch_ax_f32_lx<10>(epb, rd, a, s);
+      case 12: return batch_ax_f32_lx<12>(epb, rd, a, s);
+    }
+    return fail(NB_ERR_UNSUPPORTED, "batched solve: lx1=%d not supported", lx);
+  }
+  static int batch_ax_f64(int lx, int epb, const BaxArgs<double> &a, cudaStream_t s) {
+    switch (lx) {
+      case 4: return batch_ax_f64_lx<4>(epb, a, s);
+      case 6: return batch_ax_f64_lx<6>(epb, a, s);
+      case 8: return batch_ax_f64_lx<8>(epb, a, s);
+      case 10: return batch_ax_f64_lx<10>(epb, a, s);
+      case 12: return batch_ax_f64_lx<12>(epb, a, s);
+    }
+    return fail(NB_ERR_UNSUPPORTED, "batched solve: lx1=%d not supported", lx);
+  }
+
+  // one inner FP32 iteration / the FP64 defect, for all active problems
+  int inner_iteration(int it, cudaStream_t s) const {
+    NB_TRY(launch_inner_ax(it, s));
+    k_bgs_fin<<<ngc, kThreads, 0, s>>>(w32, p32, c32, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
+                                       part_ax, cnt);
+    NB_CUDA(cudaGetLastError());
+    k_bupd<<<npc, kThreads, 0, s>>>(e32, r32, p32, w32, c32, pch_q0, pch_prob, pb, sc, part_pt,
+                                     cnt + nprob);
+    NB_CUDA(cudaGetLastError());
+    return NB_OK;
+  }
+  int defect(double tol, int inner, int max_outer, cudaStream_t s) const {
+    NB_TRY(launch_defect_ax(s));
+    k_bgs_res<<<ngc, kThreads, 0, s>>>(w, x, f, r, c, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
+                                       part_ax, cnt + 2 * nprob, tol, inner, max_outer);
+    NB_CUDA(cudaGetLastError());
+    return NB_OK;
+  }
+
+  int build_graph(double tol, int inner, int max_outer) {
+    if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer) return NB_OK;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    if (!cap) NB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t G = nullptr;
+    NB_CUDA(cudaGraphCreate(&G, 0));
+    graph = G;
+    cudaGraphConditionalHandle h;
+    NB_CUDA(cudaGraphConditionalHandleCreate(&h, G, 0, 0));
+    const int max_cycles = max_outer + 1;
+    // initial norms, then the first value of the loop condition, captured
+    // into the graph itself (the node setting the condition must belong to
+    // the graph that owns the handle)
+    NB_CUDA(cudaStreamBeginCaptureToGraph(cap, G, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+    k_binit<<<npc, kThreads, 0, cap>>>(x, r, f, c, pch_q0, pch_prob, pb, sc, part_pt,
+                                       cnt + 3 * nprob, max_outer);
+    k_bcontrol<<<1, kThreads, 0, cap>>>(sc, nprob, cycles, 1, max_cycles, h);
+    {
+      cudaGraph_t got = nullptr;
+      NB_CUDA(cudaStreamEndCapture(cap, &got));
+    }
+    // the loop follows the capture's last node (the one without dependents)
+    size_t nn = 0;
+    NB_CUDA(cudaGraphGetNodes(G, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    NB_CUDA(cudaGraphGetNodes(G, nodes.data(), &nn));
+    cudaGraphNode_t ninit = nullptr;
+    for (cudaGraphNode_t q : nodes) {
+      size_t nd = 0;
+      NB_CUDA(cudaGraphNodeGetDependentNodes(q, nullptr, nullptr, &nd));
+      if (nd == 0) ninit = q;
+    }
+    if (nn != 2 || !ninit) return fail(NB_ERR_CUDA, "batched solve: unexpected initial graph");
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t nloop;
+    NB_CUDA(cudaGraphAddNode(&nloop, G, &ninit, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    // one cycle: scale, inner CG, FP64 defect, loop condition
+    NB_CUDA(cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+    int st = NB_OK;
+    k_bscale<<<npc, kThreads, 0, cap>>>(r32, e32, r, c32, pch_q0, pch_prob, pb, sc, part_pt,
+                                        cnt + 3 * nprob);
+    if (cudaGetLastError() != cudaSuccess) st = fail(NB_ERR_CUDA, "batched solve: capture");
+    for (int it = 1; it <= inner && !st; ++it) st = inner_iteration(it, cap);
+    if (!st) st = defect(tol, inner, max_outer, cap);
+    if (!st) {
+      k_bcontrol<<<1, kThreads, 0, cap>>>(sc, nprob, cycles, 0, max_cycles, h);
+      if (cudaGetLastError() != cudaSuccess) st = fail(NB_ERR_CUDA, "batched solve: capture");
+    }
+    cudaGraph_t got = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(cap, &got);
+    if (st) return st;
+    if (ce != cudaSuccess) return fail(NB_ERR_CUDA, "batched solve: capture: %s",
+                                       cudaGetErrorString(ce));
+    NB_CUDA(cudaGraphInstantiate(&exec, G, 0));
+    g_tol = tol;
+    g_inner = inner;
+    g_outer = max_outer;
+    return NB_OK;
+  }
+};
+
+namespace {
+
+template <typename T>
+int dalloc(T **p, size_t count) {
+  if (count == 0) count = 1;
+  if (cudaMalloc(p, count * sizeof(T)) != cudaSuccess)
+    return fail(NB_ERR_CUDA, "batched solve: out of device memory (%zu bytes)",
+                count * sizeof(T));
+  return NB_OK;
+}
+
+template <typename T>
+int upload(T **p, const std::vector<T> &h) {
+  NB_TRY(dalloc(p, h.size()));
+  if (!h.empty())
+    NB_CUDA(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return NB_OK;
+}
+
+int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz,
+                const int *lx) {
+  B->nprob = nprob;
+  B->nelx.assign(nx, nx + nprob);
+  B->nely.assign(ny, ny + nprob);
+  B->nelz.assign(nz, nz + nprob);
+  B->lx.assign(lx, lx + nprob);
+  for (int p = 0; p < nprob; ++p) {
+    if (nx[p] <= 0 || ny[p] <= 0 || nz[p] <= 0)
+      return fail(NB_ERR_ARG, "batched solve: problem %d box %dx%dx%d", p, nx[p], ny[p], nz[p]);
+    if (!(lx[p] == 4 || lx[p] == 6 || lx[p] == 8 || lx[p] == 10 || lx[p] == 12))
+      return fail(NB_ERR_UNSUPPORTED, "batched solve: problem %d lx1=%d (supported 4,6,8,10,12)",
+                  p, lx[p]);
+  }
+  // internal order: by lx1, then by user index
+  std::vector<int> order(nprob);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lx[a] < lx[b]; });
+  B->slot.assign(nprob, 0);
+  B->P_user = order;
+  for (int s = 0; s < nprob; ++s) B->slot[order[s]] = s;
+  // per-problem groups (host), built in parallel
+  std::vector<std::vector<int>> offs(nprob);
+  std::vector<std::vector<unsigned>> idxs(nprob);
+  {
+    const int nth = std::max(1, std::min<int>(nprob, int(std::thread::hardware_concurrency())));
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t)
+      th.emplace_back([&, t]() {
+        for (int s = t; s < nprob; s += nth) {
+          const int p = order[s];
+          box_groups(nx[p], ny[p], nz[p], lx[p], offs[s], idxs[s]);
+        }
+      });
+    for (auto &t : th) t.join();
+  }
+  // concatenation
+  B->P.resize(nprob);
+  std::vector<int> el_prob, off_all, gch_g0, gch_prob, pch_prob;
+  std::vector<unsigned> idx_all;
+  std::vector<long> pch_q0;
+  long pt = 0;
+  int el = 0, gbase = 0;
+  for (int s = 0; s < nprob; ++s) {
+    const int p = order[s];
+    const long l3 = long(lx[p]) * lx[p] * lx[p];
+    const long nelt = long(nx[p]) * ny[p] * nz[p];
+    if (pt + nelt * l3 >= (1L << 31) || el + nelt >= (1L << 31))
+      return fail(NB_ERR_UNSUPPORTED, "batched solve: more than 2^31-1 points in the batch");
+    BatchProb &Q = B->P[s];
+    Q.pt0 = pt;
+    Q.n = nelt * l3;
+    Q.el0 = el;
+    Q.nelt = int(nelt);
+    for (long e = 0; e < nelt; ++e) el_prob.push_back(s);
+    const int ngp = int(offs[s].size()) - 1;
+    for (int q = 0; q < ngp; ++q)
+      if (offs[s][q + 1] - offs[s][q] > 8)
+        return fail(NB_ERR_STATE, "batched solve: a boundary group of more than 8 points");
+    for (int q = 0; q < ngp; ++q) off_all.push_back(offs[s][q] + int(idx_all.size()));
+    for (unsigned m : idxs[s])
+      idx_all.push_back(unsigned(pt + (m & 0x7fffffffu)) | (m & 0x80000000u));
+    Q.gc0 = int(gch_prob.size());
+    for (int a = 0; a < ngp; a += kGroupChunk) {
+      gch_g0.push_back(gbase + a);
+      gch_prob.push_back(s);
+    }
+    Q.ngc = int(gch_prob.size()) - Q.gc0;
+    Q.pc0 = int(pch_prob.size());
+    for (long a = 0; a < Q.n; a += kPointChunk) {
+      pch_q0.push_back(pt + a);
+      pch_prob.push_back(s);
+    }
+    Q.npc = int(pch_prob.size()) - Q.pc0;
+    gbase += ngp;
+    pt += Q.n;
+    el += int(nelt);
+    if (B->groups.empty() || B->groups.back().lx != lx[p]) {
+      Batch::Group G;
+      G.lx = lx[p];
+      G.el0 = Q.el0;
+      G.pt0 = Q.pt0;
+      B->groups.push_back(G);
+    }
+    B->groups.back().nel += int(nelt);
+    B->groups.back().n += Q.n;
+  }
+  off_all.push_back(int(idx_all.size()));
+  gch_g0.push_back(gbase);
+  pch_q0.push_back(pt);
+  B->n = pt;
+  B->nelt = el;
+  B->ng = gbase;
+  B->ngc = int(gch_prob.size());
+  B->npc = int(pch_prob.size());
+  const long n = B->n;
+  NB_TRY(dalloc(&B->x, n));
+  NB_TRY(dalloc(&B->f, n));
+  NB_TRY(dalloc(&B->g, 6 * n));
+  NB_TRY(dalloc(&B->c, n));
+  NB_TRY(dalloc(&B->r, n));
+  NB_TRY(dalloc(&B->w, n));
+  NB_TRY(dalloc(&B->g32, 6 * n));
+  NB_TRY(dalloc(&B->c32, n));
+  NB_TRY(dalloc(&B->r32, n));
+  NB_TRY(dalloc(&B->e32, n));
+  NB_TRY(dalloc(&B->p32, n));
+  NB_TRY(dalloc(&B->w32, n));
+  NB_TRY(upload(&B->el_prob, el_prob));
+  NB_TRY(upload(&B->off, off_all));
+  NB_TRY(upload(&B->idx, idx_all));
+  NB_TRY(upload(&B->gch_g0, gch_g0));
+  NB_TRY(upload(&B->gch_prob, gch_prob));
+  NB_TRY(upload(&B->pch_q0, pch_q0));
+  NB_TRY(upload(&B->pch_prob, pch_prob));
+  NB_TRY(upload(&B->pb, B->P));
+  NB_TRY(dalloc(&B->sc, nprob));
+  NB_TRY(dalloc(&B->cnt, 4 * size_t(nprob)));
+  NB_TRY(dalloc(&B->cycles, 1));
+  NB_TRY(dalloc(&B->part_ax, B->nelt));
+  NB_TRY(dalloc(&B->part_gs, B->ngc));
+  NB_TRY(dalloc(&B->part_pt, B->npc));
+  NB_CUDA(cudaMemset(B->cnt, 0, 4 * size_t(nprob) * sizeof(unsigned)));
+  NB_CUDA(cudaMemset(B->sc, 0, nprob * sizeof(BatchScalars)));
+  for (auto &G : B->groups) {
+    const int L = G.lx;
+    std::vector<double> a(L * L), b(L), cc(L * L), d(L * L), zz(L);
+    semhat(a.data(), b.data(), cc.data(), d.data(), zz.data(), L - 1);
+    std::vector<float> d32(d.begin(), d.end());
+    NB_TRY(upload(&G.D64, d));
+    NB_TRY(upload(&G.D32, d32));
+    // default shape: the single-mesh operator's (one element per block,
+    // register D for FP32) where instantiated, else the smallest count
+    const auto s32 = batch_shapes_f32(L);
+    const auto s64 = batch_shapes_f64(L);
+    G.tune.epb32 = s32.front().first;
+    G.tune.rd32 = 1;
+    G.tune.epb64 = s64.front();
+  }
+  return NB_OK;
+}
+
+}  // namespace
+
+std::vector<std::pair<int, int>> batch_shapes_f32(int lx) {
+  std::vector<int> e;
+  switch (lx) {
+    case 4: e = {4, 8, 16}; break;
+    case 6: e = {2, 4, 8}; break;
+    default: e = {1, 2, 4}; break;
+  }
+  std::vector<std::pair<int, int>> out;
+  for (int rd = 1; rd >= 0; --rd)
+    for (int v : e) out.push_back({v, rd});
+  // order: register-D shapes first, smallest element count first
+  std::stable_sort(out.begin(), out.end(), [](const std::pair<int, int> &a,
+                                               const std::pair<int, int> &b) {
+    return a.second > b.second;
+  });
+  return out;
+}
+
+std::vector<int> batch_shapes_f64(int lx) {
+  switch (lx) {
+    case 4: return {4, 8};
+    case 6: return {2, 4};
+    default: return {1, 2};
+  }
+}
+
+}  // namespace nb
+
+using namespace nb;
+
+struct nb_batch {
+  Batch B;
+};
+
+extern "C" {
+
+int nb_batch_create(nb_batch **out, int nprob, const int *nelx, const int *nely,
+                    const int *nelz, const int *lx1) {
+  clear_status();
+  if (!out) return fail(NB_ERR_ARG, "nb_batch_create: null output");
+  *out = nullptr;
+  if (nprob <= 0 || !nelx || !nely || !nelz || !lx1)
+    return fail(NB_ERR_ARG, "nb_batch_create: %d problems", nprob);
+  nb_batch *b = new nb_batch();
+  const int st = batch_build(&b->B, nprob, nelx, nely, nelz, lx1);
+  if (st) {
+    delete b;
+    return st;
+  }
+  *out = b;
+  return NB_OK;
+}
+
+int nb_batch_destroy(nb_batch *b) {
+  clear_status();
+  if (!b) return NB_OK;
+  cudaStreamSynchronize(lib_stream());
+  delete b;
+  return NB_OK;
+}
+
+int nb_batch_info(const nb_batch *b, long *npts, int *nelt, int *nlx) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  if (npts) *npts = b->B.n;
+  if (nelt) *nelt = b->B.nelt;
+  if (nlx) *nlx = int(b->B.groups.size());
+  return NB_OK;
+}
+
+int nb_batch_problem(const nb_batch *b, int prob, long *pt_offset, long *npts, int *lx1) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  if (prob < 0 || prob >= b->B.nprob) return fail(NB_ERR_ARG, "problem %d out of range", prob);
+  const BatchProb &Q = b->B.P[b->B.slot[prob]];
+  if (pt_offset) *pt_offset = Q.pt0;
+  if (npts) *npts = Q.n;
+  if (lx1) *lx1 = b->B.lx[prob];
+  return NB_OK;
+}
+
+int nb_batch_arrays(nb_batch *b, double **x, double **f, double **g, double **c) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  if (x) *x = b->B.x;
+  if (f) *f = b->B.f;
+  if (g) *g = b->B.g;
+  if (c) *c = b->B.c;
+  return NB_OK;
+}
+
+int nb_batch_setup(nb_batch *b, uint64_t seed) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  Batch &B = b->B;
+  cudaStream_t s = lib_stream();
+  for (auto &G : B.groups) {
+    const int L = G.lx;
+    std::vector<double> a(L * L), wb(L), cc(L * L), d(L * L), zz(L);
+    semhat(a.data(), wb.data(), cc.data(), d.data(), zz.data(), L - 1);
+    double *dw = nullptr;
+    NB_TRY(upload(&dw, wb));
+    k_bsetup_g<<<grid_for(G.n), 256, 0, s>>>(B.g + 6 * G.pt0, dw, L, G.n);
+    const cudaError_t e = cudaGetLastError();
+    NB_CUDA(cudaStreamSynchronize(s));
+    cudaFree(dw);
+    if (e != cudaSuccess) return fail(NB_ERR_CUDA, "nb_batch_setup: %s", cudaGetErrorString(e));
+  }
+  k_fill<<<grid_for(B.n), 256, 0, s>>>(B.c, 1.0, B.n);
+  k_bmult<<<grid_for(B.ng), 256, 0, s>>>(B.c, B.off, B.idx, B.ng);
+  for (int p = 0; p < B.nprob; ++p) {
+    const BatchProb &Q = B.P[B.slot[p]];
+    k_brhs<<<grid_for(Q.n), 256, 0, s>>>(B.f + Q.pt0, B.lx[p], B.nelx[p], B.nely[p], Q.n,
+                                         seed + uint64_t(p));
+  }
+  k_bdssum_c_mask<<<grid_for(B.ng), 256, 0, s>>>(B.f, B.c, B.off, B.idx, B.ng);
+  k_conv<float, double><<<grid_for(6 * B.n), 256, 0, s>>>(B.g32, B.g, 6 * B.n);
+  k_conv<float, double><<<grid_for(B.n), 256, 0, s>>>(B.c32, B.c, B.n);
+  NB_CUDA(cudaGetLastError());
+  NB_CUDA(cudaStreamSynchronize(s));
+  B.setup_done = true;
+  return NB_OK;
+}
+
+int nb_batch_set_tuning(nb_batch *b, int lx1, int epb32, int rd32, int epb64) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  for (auto &G : b->B.groups)
+    if (G.lx == lx1) {
+      bool ok32 = false, ok64 = false;
+      for (auto sh : batch_shapes_f32(lx1)) ok32 |= sh.first == epb32 && sh.second == (rd32 != 0);
+      for (int v : batch_shapes_f64(lx1)) ok64 |= v == epb64;
+      if (!ok32 || !ok64)
+        return fail(NB_ERR_UNSUPPORTED, "nb_batch_set_tuning: shape not instantiated for lx1=%d",
+                    lx1);
+      G.tune.epb32 = epb32;
+      G.tune.rd32 = rd32 != 0;
+      G.tune.epb64 = epb64;
+      if (b->B.exec) {
+        cudaGraphExecDestroy(b->B.exec);
+        b->B.exec = nullptr;
+      }
+      return NB_OK;
+    }
+  return fail(NB_ERR_ARG, "nb_batch_set_tuning: no problem with lx1=%d", lx1);
+}
+
+int nb_batch_get_tuning(const nb_batch *b, int lx1, int *epb32, int *rd32, int *epb64,
+                        float *ms32, float *ms64) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  for (const auto &G : b->B.groups)
+    if (G.lx == lx1) {
+      if (epb32) *epb32 = G.tune.epb32;
+      if (rd32) *rd32 = G.tune.rd32;
+      if (epb64) *epb64 = G.tune.epb64;
+      if (ms32) *ms32 = G.tune.ms32;
+      if (ms64) *ms64 = G.tune.ms64;
+      return NB_OK;
+    }
+  return fail(NB_ERR_ARG, "nb_batch_get_tuning: no problem with lx1=%d", lx1);
+}
+
+// The autotuner: every instantiated shape of the FP32 inner operator and of
+// the FP64 defect operator is timed on the batch's own elements of each
+// lx1 (CUDA events, reps launches after one warm-up), the fastest kept.
+int nb_batch_tune(nb_batch *b, int reps) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  Batch &B = b->B;
+  if (!B.setup_done) return fail(NB_ERR_STATE, "nb_batch_tune: call nb_batch_setup first");
+  if (reps < 1) reps = 1;
+  cudaStream_t s = lib_stream();
+  // scratch state: every problem active, inputs zeroed
+  NB_CUDA(cudaMemsetAsync(B.p32, 0, B.n * sizeof(float), s));
+  NB_CUDA(cudaMemsetAsync(B.r32, 0, B.n * sizeof(float), s));
+  NB_CUDA(cudaMemsetAsync(B.e32, 0, B.n * sizeof(float), s));
+  NB_CUDA(cudaMemsetAsync(B.x, 0, B.n * sizeof(double), s));
+  k_set_active<<<(B.nprob + 255) / 256, 256, 0, s>>>(B.sc, B.nprob);
+  NB_CUDA(cudaGetLastError());
+  cudaEvent_t e0, e1;
+  NB_CUDA(cudaEventCreate(&e0));
+  NB_CUDA(cudaEventCreate(&e1));
+  int st = NB_OK;
+  for (auto &G : B.groups) {
+    float best = 1e30f;
+    BatchTune t = G.tune;
+    for (auto sh : batch_shapes_f32(G.lx)) {
+      BaxArgs<float> a{};
+      a.w = B.w32;
+      a.u = B.r32;
+      a.p = B.p32;
+      a.g = B.g32;
+      a.c = B.c32;
+      a.D = G.D32;
+      a.el_prob = B.el_prob;
+      a.sc = B.sc;
+      a.partial = B.part_ax;
+      a.pt0 = G.pt0;
+      a.el0 = G.el0;
+      a.nel = G.nel;
+      a.first = 0;
+      st = Batch::batch_ax_f32(G.lx, sh.first, sh.second, a, s);
+      if (st) break;
+      cudaEventRecord(e0, s);
+      for (int q = 0; q < reps; ++q) Batch::batch_ax_f32(G.lx, sh.first, sh.second, a, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (ms < best) {
+        best = ms;
+        t.epb32 = sh.first;
+        t.rd32 = sh.second;
+        t.ms32 = ms;
+      }
+    }
+    if (st) break;
+    best = 1e30f;
+    for (int epb : batch_shapes_f64(G.lx)) {
+      BaxArgs<double> a{};
+      a.w = B.w;
+      a.p = B.x;
+      a.g = B.g;
+      a.c = B.c;
+      a.D = G.D64;
+      a.f = B.f;
+      a.r = B.r;
+      a.e = B.e32;
+      a.el_prob = B.el_prob;
+      a.sc = B.sc;
+      a.partial = B.part_ax;
+      a.pt0 = G.pt0;
+      a.el0 = G.el0;
+      a.nel = G.nel;
+      st = Batch::batch_ax_f64(G.lx, epb, a, s);
+      if (st) break;
+      cudaEventRecord(e0, s);
+      for (int q = 0; q < reps; ++q) Batch::batch_ax_f64(G.lx, epb, a, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      ms /= reps;
+      if (ms < best) {
+        best = ms;
+        t.epb64 = epb;
+        t.ms64 = ms;
+      }
+    }
+    if (st) break;
+    G.tune = t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  NB_CUDA(cudaStreamSynchronize(s));
+  NB_CUDA(cudaGetLastError());
+  if (B.exec) {
+    cudaGraphExecDestroy(B.exec);
+    B.exec = nullptr;
+  }
+  return NB_OK;
+}
+
+// Enqueues the whole solve (one graph launch) on the library stream.
+int nb_batch_solve(nb_batch *b, double tol, int inner_iters, int max_outer) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  Batch &B = b->B;
+  if (!B.setup_done) return fail(NB_ERR_STATE, "nb_batch_solve: call nb_batch_setup first");
+  if (inner_iters < 1 || max_outer < 0 || !(tol >= 0.0))
+    return fail(NB_ERR_ARG, "nb_batch_solve: inner_iters=%d max_outer=%d", inner_iters,
+                max_outer);
+  NB_TRY(B.build_graph(tol, inner_iters, max_outer));
+  NB_CUDA(cudaGraphLaunch(B.exec, lib_stream()));
+  return NB_OK;
+}
+
+int nb_batch_result(const nb_batch *b, int prob, int *outer, int *inner, double *relres) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  if (prob < 0 || prob >= b->B.nprob) return fail(NB_ERR_ARG, "problem %d out of range", prob);
+  BatchScalars S;
+  cudaStream_t s = lib_stream();
+  NB_CUDA(cudaMemcpyAsync(&S, b->B.sc + b->B.slot[prob], sizeof(S), cudaMemcpyDeviceToHost, s));
+  NB_CUDA(cudaStreamSynchronize(s));
+  if (outer) *outer = S.outer;
+  if (inner) *inner = S.inner;
+  if (relres) *relres = S.rn0 > 0 ? S.rn / S.rn0 : 0.0;
+  return NB_OK;
+}
+
+int nb_batch_cycles(const nb_batch *b, int *cycles) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  int v = 0;
+  cudaStream_t s = lib_stream();
+  NB_CUDA(cudaMemcpyAsync(&v, b->B.cycles, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NB_CUDA(cudaStreamSynchronize(s));
+  if (cycles) *cycles = v;
+  return NB_OK;
+}
+
+// Host <-> device copies of the concatenated right-hand side and solution
+// (problem p at nb_batch_problem's offset), asynchronous on the library
+// stream: host buffers should be pinned.
+int nb_batch_rhs_in(nb_batch *b, const double *f_host) {
+  clear_status();
+  if (!b || !f_host) return fail(NB_ERR_ARG, "nb_batch_rhs_in: null argument");
+  NB_CUDA(cudaMemcpyAsync(b->B.f, f_host, b->B.n * sizeof(double), cudaMemcpyHostToDevice,
+                          lib_stream()));
+  return NB_OK;
+}
+
+int nb_batch_x_out(nb_batch *b, double *x_host) {
+  clear_status();
+  if (!b || !x_host) return fail(NB_ERR_ARG, "nb_batch_x_out: null argument");
+  NB_CUDA(cudaMemcpyAsync(x_host, b->B.x, b->B.n * sizeof(double), cudaMemcpyDeviceToHost,
+                          lib_stream()));
+  return NB_OK;
+}
+
+}  // extern "C"

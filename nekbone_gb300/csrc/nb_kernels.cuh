@@ -26,6 +26,15 @@ template <typename T> struct Vec2;
 template <> struct Vec2<double> { typedef double2 type; };
 template <> struct Vec2<float> { typedef float2 type; };
 
+// counter-based uniform [-1,1) keyed by (seed, global id): splitmix64 finaliser
+__device__ __forceinline__ double uniform_pm1(uint64_t seed, uint64_t id) {
+  uint64_t z = seed * 0x9E3779B97F4A7C15ull + id + 0x632BE59BD9B4E019ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z = z ^ (z >> 31);
+  return double(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
 // ------------------------------------------------------------ reduction --
 // Deterministic block sum of one value per thread: a fixed shuffle tree in
 // the accumulation type A (float for the FP32 kernels, which keeps FP64

@@ -37,15 +37,6 @@ __global__ void k_setup_g(double *g, const double *wgt, int lx, long n) {
   }
 }
 
-// counter-based uniform [-1,1) keyed by (seed, global id): splitmix64 finaliser
-__device__ __forceinline__ double uniform_pm1(uint64_t seed, uint64_t id) {
-  uint64_t z = seed * 0x9E3779B97F4A7C15ull + id + 0x632BE59BD9B4E019ull;
-  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-  z = z ^ (z >> 31);
-  return double(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
-}
-
 // box global id of local point q (set_vert_box, prox_dssum.f:42-73) for the
 // brick order lglel(e) = e
 __global__ void k_rhs_uniform(double *f, int lx, int nelx, int nely, long n,

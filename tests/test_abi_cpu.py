@@ -77,3 +77,15 @@ def test_reference_error_mode_exits_with_status_1(tmp_path):
     assert p.returncode == 1
     assert "invalid handle" in p.stderr
     assert "not reached" not in p.stdout
+
+
+def test_batch_rejects_bad_problems_without_a_gpu():
+    """nb_batch_create validates every problem before it touches the device."""
+    import nekbone_gb300 as nb
+    with pytest.raises(nb.NekboneError) as e:
+        nb.Batch([(2, 2, 2, 6), (2, 2, 2, 5)])      # lx1=5 has no batched kernel
+    assert e.value.status != 0
+    with pytest.raises(nb.NekboneError):
+        nb.Batch([(0, 2, 2, 6)])
+    with pytest.raises(nb.NekboneError):
+        nb.Batch([])
