@@ -40,6 +40,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "GDOF·iter/s (lx1=12, 32^3 elems); mixed vs FP64 GPU time to rel. resid 1e-10"
+# FP64 FMA throughput of one GB300 (an FMA-chain probe: 1/72 of FP32)
+FP64_PEAK_TFLOPS = 1.055
+# DRAM read + write bytes per point of k_ax_eo<12,1> (ncu, 16^3 elements:
+# 500.3 MB + 98.4 MB over 7,077,888 points); the kernel streams, so traffic
+# scales with n
+DRAM_BYTES_PER_POINT_AX_EO = (500.333824e6 + 98.385920e6) / 7077888
 UNIT = "GDOF*iter/s"
 
 
@@ -58,7 +64,10 @@ def parse():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-sample-nel", type=int, default=16)
-    ap.add_argument("--cpu-sample-iters", type=int, default=100)
+    ap.add_argument("--cpu-sample-iters", type=int, default=250)
+    ap.add_argument("--case", choices=["cg", "tc", "batch"], default="cg",
+                    help="cg: the benchmark; tc / batch: a small case of the tensor-core "
+                         "operator / the batched solver, for profiling")
     return ap.parse_args()
 
 
@@ -253,7 +262,83 @@ def extras(nb, torch, dev):
                                                      "setup_s": tset}
     res["hsmg_pcg"]["workload"] = "16^3 deformed elements, lx1=12, levels 12->6->3, tol 1e-10"
     m.close()
+    del g, c, f, x
+    torch.cuda.empty_cache()
+    res["batched_uneven"] = batched(nb, torch, dev)
     return res
+
+
+def batch_boxes(nprob=256, seed=4096):
+    """The batched workload: element counts log-uniform in [8, 4096]
+    factorised by cubic (driver.f:196-247), lx1 uniform over {6, 8, 10, 12}."""
+    import nekbone_gb300 as nb
+    rng = np.random.default_rng(seed)
+    e = np.rint(np.exp(rng.uniform(np.log(8), np.log(4096), nprob))).astype(int)
+    lx = rng.choice([6, 8, 10, 12], nprob)
+    return [(*nb.cubic(int(ei)), int(li)) for ei, li in zip(e, lx)]
+
+
+def batched(nb, torch, dev, reps=3):
+    """256 independent Dirichlet problems solved to 1e-10 by one graph launch
+    (FP32 inner CG, 20 iterations per cycle, FP64 defect correction), after
+    the autotuner picked each lx1's operator shapes."""
+    boxes = batch_boxes()
+    t0 = time.perf_counter()
+    b = nb.Batch(boxes)
+    b.setup(777)
+    setup_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.tune(3)
+    tune_s = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
+    b.solve(1e-10, 20, 60)       # warm-up (builds and instantiates the graph)
+    nb.sync()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.solve(1e-10, 20, 60)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    res = [b.result(p) for p in range(b.nprob)]
+    work = sum(b.problem(p)[1] * res[p][1] for p in range(b.nprob))
+    # end to end: pinned host f in, solve, x out
+    fh = torch.empty(b.n, dtype=torch.float64).pin_memory()
+    xh = torch.empty(b.n, dtype=torch.float64).pin_memory()
+    fdev = torch.as_tensor(_DevArray(b.arrays()[1], b.n), device=dev)
+    fh.copy_(fdev.cpu())
+    nb.sync()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        b.rhs_in(fh.data_ptr())
+        b.solve(1e-10, 20, 60)
+        b.x_out(xh.data_ptr())
+        nb.sync()
+    e2e_ms = (time.perf_counter() - t0) / reps * 1e3
+    lxs = sorted({bx[3] for bx in boxes})
+    out = {
+        "workload": "256 box problems, elements log-uniform in [8,4096] (cubic factorisation), "
+                    "lx1 uniform over {6,8,10,12}, seeded uniform RHS, full Dirichlet mask; "
+                    "FP32 inner CG (20 iterations per cycle) in FP64 defect correction to 1e-10",
+        "problems": b.nprob, "points": b.n, "elements": b.nelt, "setup_s": setup_s,
+        "tune_s": tune_s, "tuning": {str(l): b.tuning(l) for l in lxs},
+        "solve_ms": ms, "graph_launches_per_solve": 1, "cycles": b.cycles(),
+        "max_relres": max(r[2] for r in res), "max_outer": max(r[0] for r in res),
+        "min_outer": min(r[0] for r in res),
+        "inner_gdof_iter_per_s": work / (ms * 1e-3) / 1e9,
+        "e2e_ms": e2e_ms, "e2e_h2d_bytes": 8 * b.n, "e2e_d2h_bytes": 8 * b.n,
+    }
+    b.close()
+    return out
+
+
+class _DevArray:
+    """A float64 device array given by pointer, for torch.as_tensor."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8",
+                                         "data": (ptr, False), "version": 3}
 
 
 # --------------------------------------------------------------- GPU arm --
@@ -319,12 +404,21 @@ def run_ours(a, rank, world, local):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = ax_bytes / (kms[0] * 1e-3) / 1e9
     flops_pt = 19 + 12 * lx
+    eo = lx % 2 == 0
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
-                "kernel": "k_ax<double,12,1> (fused element operator)",
+                "frac": achieved / peak,
+                # DRAM bytes per launch: ncu capture of the same kernel on 16^3
+                # elements (84.6 B per point read + written), scaled by n
+                "traffic": DRAM_BYTES_PER_POINT_AX_EO * n if (eo and lx == 12) else None,
+                "kernel": f"k_ax_eo<{lx},1> (fused element operator, even-odd contractions)"
+                          if eo else f"k_ax_impl<double,{lx},1,false> (fused element operator)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                 "kernel_ms": {"ax": kms[0], "gs_fin": kms[1], "update": kms[2]},
-                "fp64_tflops": flops_pt * n / (kms[0] * 1e-3) / 1e12}
+                # the binding resource: the FP64 pipe (GB300 FP64 = 1/72 of FP32)
+                "fp64_pipe": {"reference_flops_per_point": flops_pt,
+                              "tflops_reference_count": flops_pt * n / (kms[0] * 1e-3) / 1e12,
+                              "peak_tflops": FP64_PEAK_TFLOPS,
+                              "ncu_pipe_active": 0.904 if (eo and lx == 12) else None}}
 
     # the FP32 iteration of the mixed solver's inner CG, same mesh
     f32, g32, c32 = f.float(), g.float(), c.float()
@@ -408,11 +502,51 @@ def run_ours(a, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+def run_case(a):
+    """Small cases for kernel profiles (one JSON line of timings, not a bench
+    line): 'tc' applies the tensor-core and CUDA-core FP32 operators on 16^3
+    deformed elements (lx1 = --lx); 'batch' solves the first 32 problems of
+    the batched workload once after tuning."""
+    import torch
+    import nekbone_gb300 as nb
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(0)
+    stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
+    if a.case == "tc":
+        m = nb.DeviceMesh(16, 16, 16, a.lx, mask_mode=1)
+        n = m.n
+        g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+        m.setup_g_deformed(g.data_ptr(), 11, 0.1)
+        g32 = g.float()
+        u = torch.rand(n, dtype=torch.float32, device=dev)
+        w = torch.empty_like(u)
+        torch.cuda.synchronize()
+        out = {"case": "tc", "n": n, "lx": a.lx,
+               "tc_ms": _time_on(stream, torch, lambda: m.ax_tc(w.data_ptr(), u.data_ptr(),
+                                                                g32.data_ptr()), reps=3),
+               "fp32_ms": _time_on(stream, torch, lambda: m.ax_f32(w.data_ptr(), u.data_ptr(),
+                                                                   g32.data_ptr()), reps=3)}
+    else:
+        b = nb.Batch(batch_boxes()[:32])
+        b.setup(777)
+        b.tune(1)
+        torch.cuda.synchronize()
+        b.solve(1e-10, 20, 60)
+        nb.sync()
+        out = {"case": "batch", "problems": b.nprob, "points": b.n, "cycles": b.cycles(),
+               "max_relres": max(b.result(p)[2] for p in range(b.nprob))}
+        b.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
     if a.impl == "reference":
         run_reference(a, rank, world)
+        return
+    if a.case != "cg":
+        run_case(a)
         return
     run_ours(a, rank, world, local)
 
