@@ -12,13 +12,18 @@
  *     own jl library (src/jl/gs.c, src/jl/gs_local.c) compiled from the
  *     reference sources into oracle/_ref/ by oracle/Makefile, and against the
  *     known answers of src/jl/gs_test.c.
- *   - GLL / derivative matrices (orc_zwgll, orc_semhat): pinned against closed
- *     forms and polynomial-exactness identities (no Fortran compiler exists in
- *     this image to run src/speclib.f itself).
- *   - ax / cg / hsmg: parity unpinned -- the reference is Fortran 77 and no
- *     Fortran compiler is available, so these follow the reference source line
- *     by line (citations at each function) and are checked by mathematical
- *     identities only.
+ *   - everything restated from the Fortran sources -- GLL points, semhat,
+ *     cubic, set_vert_box, setup_g, set_multiplicity, set_f, ax with the
+ *     reference's maskit, the driver's two cg calls with every glsc3 value,
+ *     and hsmg: pinned against golden vectors from the reference's own
+ *     Fortran sources executed by oracle/f77.py, a Fortran 77 subset
+ *     executor (no Fortran compiler exists in this image), with the
+ *     reference's jl library for gather-scatter
+ *     (tests/golden/make_golden_fortran.py).  The plain build (ORC_FMA=0)
+ *     reproduces them bit for bit, including the C1 configuration (4^3
+ *     elements, lx1=10, 2 x 100 iterations).  hsmg agrees to 1e-12: its
+ *     generalised eigenproblems are solved by a different eigensolver
+ *     (Jacobi here, LAPACK dsygv there).
  *
  * Arrays follow the reference's Fortran layout (column-major, element-major,
  * i fastest) with 0-based C indexing.
