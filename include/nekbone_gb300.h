@@ -148,6 +148,21 @@ typedef struct nb_mesh nb_mesh;
 int  nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
                     int mask_mode);
 int  nb_mesh_destroy(nb_mesh *mesh);
+/* Where nb_mesh_create builds a full-mask mesh's topology: 1 (default) on
+ * the device, without a sort (closed-form copies of each box point, jl's
+ * group and member order); 0 on the host with jl's sort-based construction
+ * (gs_setup, jl/gs.c:88-113, 330-357).  Both give identical maps. */
+void nb_set_setup_on_device(int on);
+/* The mesh's gather-scatter groups (jl order: groups by primary, members
+ * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)
+ * are filled when given. */
+int nb_mesh_gs_maps(const nb_mesh *mesh, int *ng, long *nmem, int *off, int *idx);
+/* The fused pass's element-boundary groups (singletons included), members
+ * on a domain face flagged in bit 31. */
+int nb_mesh_boundary_groups(const nb_mesh *mesh, int *nbg, long *nmem, int *off,
+                            unsigned *idx);
+/* The mesh's masked local indices (ascending). */
+int nb_mesh_mask_list(const nb_mesh *mesh, int *n, int *list);
 /* contraction order of this mesh's FP64 operator (see
  * nekbone_set_contraction_order_) */
 int  nb_mesh_set_order(nb_mesh *mesh, int order);

@@ -53,7 +53,8 @@ EXPORTS = (
     "nb_batch_create", "nb_batch_destroy", "nb_batch_info", "nb_batch_problem",
     "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
-    "nb_batch_rhs_in", "nb_batch_x_out",
+    "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_mesh_gs_maps",
+    "nb_mesh_boundary_groups", "nb_mesh_mask_list",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -116,6 +117,13 @@ for _name, _args in (
         ("nb_batch_x_out", [_p, _p])):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = _args
+lib.nb_set_setup_on_device.restype = None
+lib.nb_set_setup_on_device.argtypes = [_i]
+for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
+    getattr(lib, _name).restype = _i
+    getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
+lib.nb_mesh_mask_list.restype = _i
+lib.nb_mesh_mask_list.argtypes = [_p, _p, _p]
 #: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
 NOALLOC_MAX_N = 67108864
 
@@ -397,6 +405,31 @@ class DeviceMesh:
         except Exception:
             pass
 
+    def gs_maps(self):
+        """(off, idx) of the gather-scatter groups (int32 numpy arrays)."""
+        ng, nm = _C.c_int(), _C.c_long()
+        _check(lib.nb_mesh_gs_maps(self._h, _C.byref(ng), _C.byref(nm), None, None))
+        off = _np.zeros(ng.value + 1, dtype=_np.int32)
+        idx = _np.zeros(max(nm.value, 1), dtype=_np.int32)
+        _check(lib.nb_mesh_gs_maps(self._h, None, None, _ptr(off), _ptr(idx)))
+        return off, idx[:nm.value]
+
+    def boundary_groups(self):
+        """(off, idx) of the fused boundary groups (idx uint32, bit 31 = masked)."""
+        ng, nm = _C.c_int(), _C.c_long()
+        _check(lib.nb_mesh_boundary_groups(self._h, _C.byref(ng), _C.byref(nm), None, None))
+        off = _np.zeros(ng.value + 1, dtype=_np.int32)
+        idx = _np.zeros(max(nm.value, 1), dtype=_np.uint32)
+        _check(lib.nb_mesh_boundary_groups(self._h, None, None, _ptr(off), _ptr(idx)))
+        return off, idx[:nm.value]
+
+    def mask_list(self):
+        n = _C.c_int()
+        _check(lib.nb_mesh_mask_list(self._h, _C.byref(n), None))
+        out = _np.zeros(max(n.value, 1), dtype=_np.int32)
+        _check(lib.nb_mesh_mask_list(self._h, None, _ptr(out)))
+        return out[:n.value]
+
     def set_order(self, order: int) -> None:
         _check(lib.nb_mesh_set_order(self._h, order))
 
@@ -556,6 +589,11 @@ class Batch:
 
     def x_out(self, host_ptr: int) -> None:
         _check(lib.nb_batch_x_out(self._h, _C.c_void_p(host_ptr)))
+
+
+def set_setup_on_device(on: bool) -> None:
+    """Build full-mask mesh topologies on the device (default) or the host."""
+    lib.nb_set_setup_on_device(1 if on else 0)
 
 
 def tc_selftest(bf16: bool = False) -> int:

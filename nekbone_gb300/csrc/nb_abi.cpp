@@ -708,6 +708,52 @@ int nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
   return NB_OK;
 }
 
+void nb_set_setup_on_device(int on) { set_setup_on_device(on != 0); }
+
+// Copies one device int array (count entries) to host, when dst is given.
+static int copy_out(void *dst, const void *src, size_t bytes) {
+  if (!dst || !bytes) return NB_OK;
+  NB_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st().s));
+  NB_CUDA(cudaStreamSynchronize(st().s));
+  return NB_OK;
+}
+
+int nb_mesh_gs_maps(const nb_mesh *mesh, int *ng, long *nmem, int *off, int *idx) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  const GsDevice &g = mesh->op.gs;
+  if (!g.symmetric) return fail(NB_ERR_STATE, "nb_mesh_gs_maps: flagged ids (no symmetric map)");
+  int end = 0;
+  if (g.ng >= 0) NB_TRY(copy_out(&end, g.off + g.ng, sizeof(int)));
+  if (ng) *ng = g.ng;
+  if (nmem) *nmem = end;
+  NB_TRY(copy_out(off, g.off, size_t(g.ng + 1) * sizeof(int)));
+  NB_TRY(copy_out(idx, g.idx, size_t(end) * sizeof(int)));
+  return NB_OK;
+}
+
+int nb_mesh_boundary_groups(const nb_mesh *mesh, int *nbg, long *nmem, int *off,
+                            unsigned *idx) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  const Operator &op = mesh->op;
+  if (!op.fused_ok || !op.bnd_off) return fail(NB_ERR_STATE, "no fused boundary groups");
+  int end = 0;
+  NB_TRY(copy_out(&end, op.bnd_off + op.nbg, sizeof(int)));
+  if (nbg) *nbg = op.nbg;
+  if (nmem) *nmem = end;
+  NB_TRY(copy_out(off, op.bnd_off, size_t(op.nbg + 1) * sizeof(int)));
+  NB_TRY(copy_out(idx, op.bnd_idx, size_t(end) * sizeof(unsigned)));
+  return NB_OK;
+}
+
+int nb_mesh_mask_list(const nb_mesh *mesh, int *n, int *list) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (n) *n = mesh->op.n_mask;
+  return copy_out(list, mesh->op.d_mask_list, size_t(mesh->op.n_mask) * sizeof(int));
+}
+
 int nb_mesh_set_order(nb_mesh *mesh, int order) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");

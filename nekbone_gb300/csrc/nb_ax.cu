@@ -9,6 +9,8 @@ int launch_ax_f64_m2(int lx, AxArgs<double> a, cudaStream_t s);
 int launch_ax_eo_m0(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
 int launch_ax_eo_m1(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
 int launch_ax_eo_m2(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
+int launch_ax_eo32_m0(int lx, AxArgs<float> a, const float *eo, cudaStream_t s);
+int launch_ax_eo32_m1(int lx, AxArgs<float> a, const float *eo, cudaStream_t s);
 int launch_ax_f32_m0(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m1(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m2(int lx, AxArgs<float> a, cudaStream_t s);
@@ -31,6 +33,10 @@ template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
+  if (op.order == 1 && op.eo_ok && op.fEO && mode != 2) {  // even-odd, one line per thread
+    if (mode == 0) return launch_ax_eo32_m0(op.lx, a, op.fEO, s);
+    return launch_ax_eo32_m1(op.lx, a, op.fEO, s);
+  }
   if (mode == 0) return launch_ax_f32_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f32_m1(op.lx, a, s);
   return launch_ax_f32_m2(op.lx, a, s);

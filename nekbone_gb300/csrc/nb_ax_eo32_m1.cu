@@ -1,0 +1,8 @@
+// Even-odd FP32 element operator instantiations, mode 1 (nb_kernels.cuh).
+#include "nb_ax_eo_launch.cuh"
+
+namespace nb {
+int launch_ax_eo32_m1(int lx, AxArgs<float> a, const float *eo, cudaStream_t s) {
+  return launch_ax_eo_mode<float, 1>(lx, a, eo, s);
+}
+}  // namespace nb

@@ -1,28 +1,39 @@
-// nb_ax_eo_launch.cuh -- dispatch of the even-odd FP64 operator over even lx1.
+// nb_ax_eo_launch.cuh -- dispatch of the even-odd element operator (FP64 and
+// FP32) over even lx1.
 #pragma once
 
 #include "nb_solver.h"
 
 namespace nb {
 
-template <int LX, int MODE>
-int launch_ax_eo_lx(AxArgs<double> a, const double *eo, cudaStream_t s) {
-  const size_t sm = ax_eo_smem_bytes<LX>();
+template <typename T, int LX, int MODE, bool TMAG>
+int launch_ax_eo_shape(AxArgs<T> a, const T *eo, cudaStream_t s) {
+  const size_t sm = ax_eo_smem_bytes<T, LX, TMAG>();
   static bool attr_set = false;
   if (!attr_set) {
-    NB_CUDA(cudaFuncSetAttribute(k_ax_eo<LX, MODE>,
+    NB_CUDA(cudaFuncSetAttribute(k_ax_eo<T, LX, MODE, TMAG>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
     attr_set = true;
   }
-  k_ax_eo<LX, MODE><<<a.nelt, dim3(LX, LX), sm, s>>>(a, eo);
+  k_ax_eo<T, LX, MODE, TMAG><<<a.nelt, dim3(LX, LX), sm, s>>>(a, eo);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
 
-template <int MODE>
-int launch_ax_eo_mode(int lx, AxArgs<double> a, const double *eo, cudaStream_t s) {
+// FP32 with a 16-byte aligned metric: the bulk-copy (TMAG) form
+template <typename T, int LX, int MODE>
+int launch_ax_eo_lx(AxArgs<T> a, const T *eo, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4 && MODE != 2 && (24 * LX * LX * LX) % 16 == 0) {
+    if ((reinterpret_cast<uintptr_t>(a.g) & 15u) == 0)
+      return launch_ax_eo_shape<T, LX, MODE, true>(a, eo, s);
+  }
+  return launch_ax_eo_shape<T, LX, MODE, false>(a, eo, s);
+}
+
+template <typename T, int MODE>
+int launch_ax_eo_mode(int lx, AxArgs<T> a, const T *eo, cudaStream_t s) {
   switch (lx) {
-#define NB_CASE(L) case L: return launch_ax_eo_lx<L, MODE>(a, eo, s);
+#define NB_CASE(L) case L: return launch_ax_eo_lx<T, L, MODE>(a, eo, s);
     NB_CASE(2) NB_CASE(4) NB_CASE(6) NB_CASE(8) NB_CASE(10) NB_CASE(12) NB_CASE(14) NB_CASE(16)
 #undef NB_CASE
     default:

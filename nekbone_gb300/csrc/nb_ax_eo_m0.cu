@@ -3,6 +3,6 @@
 
 namespace nb {
 int launch_ax_eo_m0(int lx, AxArgs<double> a, const double *eo, cudaStream_t s) {
-  return launch_ax_eo_mode<0>(lx, a, eo, s);
+  return launch_ax_eo_mode<double, 0>(lx, a, eo, s);
 }
 }  // namespace nb

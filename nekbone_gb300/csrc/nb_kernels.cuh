@@ -733,14 +733,21 @@ namespace nb {
 // (j,k)=(t%n,t/n) of the r contraction, the line (i,k) of the s contraction
 // and its own column (i,j) of the t contraction (kept in registers).
 // Shared arrays use a row pitch of n+1 doubles (bank-conflict free lines).
-template <int LX>
+// TMAG: the element's metric block (6*lx1^3 values, contiguous in
+// gxyz(6,nxyz,nelt)) arrives in shared memory by one bulk copy issued when
+// the CTA starts, instead of per-point loads in the metric step -- the FP32
+// form, where those loads would otherwise wait on DRAM latency one plane at
+// a time.
+template <typename T, int LX, bool TMAG>
 struct AxEoShared {
   static constexpr int P = LX + 1;
   static constexpr int N = P * LX * LX;
-  double A[N];
-  double B[N];
-  double C[N];
-  double E4[4 * (LX / 2) * (LX / 2)];  // E, O of D, then E, O of D^T
+  alignas(128) T g[TMAG ? 6 * LX * LX * LX : 2];
+  T A[N];
+  T B[N];
+  T C[N];
+  T E4[4 * (LX / 2) * (LX / 2)];  // E, O of D, then E, O of D^T
+  alignas(8) uint64_t bar;
   double red[32];
 };
 
@@ -750,11 +757,10 @@ __device__ __forceinline__ int eo_at(int i, int j, int k) {
 }
 
 // y(0..n-1) of a folded line v (length n), coefficients Ec/Oc (h x h, row a)
-template <int LX>
-__device__ __forceinline__ void eo_line(const double *v, const double *Ec,
-                                        const double *Oc, double *y) {
+template <typename T, int LX>
+__device__ __forceinline__ void eo_line(const T *v, const T *Ec, const T *Oc, T *y) {
   constexpr int H = LX / 2;
-  double ve[H], vo[H];
+  T ve[H], vo[H];
 #pragma unroll
   for (int m = 0; m < H; ++m) {
     ve[m] = add_rn(v[m], v[LX - 1 - m]);
@@ -762,8 +768,8 @@ __device__ __forceinline__ void eo_line(const double *v, const double *Ec,
   }
 #pragma unroll
   for (int a = 0; a < H; ++a) {
-    double ye = mul_rn(Ec[a * H], ve[0]);
-    double yo = mul_rn(Oc[a * H], vo[0]);
+    T ye = mul_rn(Ec[a * H], ve[0]);
+    T yo = mul_rn(Oc[a * H], vo[0]);
 #pragma unroll
     for (int m = 1; m < H; ++m) {
       ye = fma_rn(Ec[a * H + m], ve[m], ye);
@@ -774,23 +780,29 @@ __device__ __forceinline__ void eo_line(const double *v, const double *Ec,
   }
 }
 
-template <int LX, int MODE>
+template <typename T, int LX, int MODE, bool TMAG>
 __global__ void __launch_bounds__(LX * LX)
-    k_ax_eo(AxArgs<double> a, const double *eo) {
+    k_ax_eo(AxArgs<T> a, const T *eo) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  AxEoShared<LX> &sm = *reinterpret_cast<AxEoShared<LX> *>(smem_raw);
+  AxEoShared<T, LX, TMAG> &sm = *reinterpret_cast<AxEoShared<T, LX, TMAG> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
   const int t = threadIdx.x + LX * threadIdx.y;
   const int i = threadIdx.x, j = threadIdx.y;  // own column (i,j)
   const int e = blockIdx.x;
   const size_t base = size_t(e) * L3;
-  const double *Ed = sm.E4, *Od = sm.E4 + H * H;            // of D
-  const double *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;  // of D^T
+  if (TMAG && t == 0) {
+    constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));
+    mbar_init(&sm.bar, 1);
+    mbar_arrive_expect_tx(&sm.bar, GBYTES);
+    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
+  }
+  const T *Ed = sm.E4, *Od = sm.E4 + H * H;            // of D
+  const T *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;  // of D^T
 
   for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = eo[q];
 
   const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
-  double creg[LX], freg[LX];
+  T creg[LX], freg[LX];
   if (MODE != 0 && col_interior) {
 #pragma unroll
     for (int k = 1; k < LX - 1; ++k) {
@@ -799,17 +811,17 @@ __global__ void __launch_bounds__(LX * LX)
       if (MODE == 2) freg[k] = a.f[id];
     }
   }
-  double ureg[LX], pold[LX];
-  const double beta = (MODE == 1 && !a.first) ? a.sc->beta : 0.0;
+  T ureg[LX], pold[LX];
+  const T beta = (MODE == 1 && !a.first) ? T(a.sc->beta) : T(0);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {  // all loads before the first store
     const size_t id = base + size_t(k) * L2 + t;
     if (MODE == 1) {
       ureg[k] = a.u[id];
-      pold[k] = a.first ? 0.0 : a.p[id];
+      pold[k] = a.first ? T(0) : a.p[id];
     } else if (MODE == 2) {
       ureg[k] = a.p[id];
-      pold[k] = a.e ? double(a.e[id]) : 0.0;
+      pold[k] = a.e ? T(a.e[id]) : T(0);
     } else {
       ureg[k] = a.u[id];
     }
@@ -821,7 +833,7 @@ __global__ void __launch_bounds__(LX * LX)
       if (!a.first) ureg[k] = fma_rn(beta, pold[k], ureg[k]);  // add2s1, math.f:534
       a.p[id] = ureg[k];
     } else if (MODE == 2 && a.e) {
-      ureg[k] = fma_rn(a.scale, pold[k], ureg[k]);
+      ureg[k] = fma_rn(T(a.scale), pold[k], ureg[k]);
       a.p[id] = ureg[k];
     }
     sm.A[eo_at<LX>(i, j, k)] = ureg[k];
@@ -831,37 +843,40 @@ __global__ void __launch_bounds__(LX * LX)
   // gradient (local_grad3, cg.f:170-187) as three folded contractions
   {
     const int l0 = t % LX, l1 = t / LX;
-    double v[LX], y[LX];
+    T v[LX], y[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(m, l0, l1)];  // line (j,k)
-    eo_line<LX>(v, Ed, Od, y);
+    eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
     for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(m, l0, l1)] = y[m];  // ur
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(l0, m, l1)];  // line (i,k)
-    eo_line<LX>(v, Ed, Od, y);
+    eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
     for (int m = 0; m < LX; ++m) sm.C[eo_at<LX>(l0, m, l1)] = y[m];  // us
   }
-  double wtreg[LX];
-  eo_line<LX>(ureg, Ed, Od, wtreg);  // ut of the own column
+  T wtreg[LX];
+  eo_line<T, LX>(ureg, Ed, Od, wtreg);  // ut of the own column
   __syncthreads();
 
   // metric, cg.f:156-163 (wr, ws back into B, C; wt in registers)
+  if (TMAG) mbar_wait_bounded(&sm.bar, 0, a.err);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = eo_at<LX>(i, j, k);
-    const double ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
+    const T ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
     const size_t pt = base + size_t(k) * L2 + t;
-    const double2 *gp = reinterpret_cast<const double2 *>(a.g + 6 * pt);
-    const double2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
-    double wr = mul_rn(g01.x, ur);
+    typedef typename Vec2<T>::type V2;
+    const V2 *gp = TMAG ? reinterpret_cast<const V2 *>(&sm.g[6 * (k * L2 + t)])
+                        : reinterpret_cast<const V2 *>(a.g + 6 * pt);
+    const V2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
+    T wr = mul_rn(g01.x, ur);
     wr = fma_rn(g01.y, us, wr);
     wr = fma_rn(g23.x, ut, wr);
-    double ws = mul_rn(g01.y, ur);
+    T ws = mul_rn(g01.y, ur);
     ws = fma_rn(g23.y, us, ws);
     ws = fma_rn(g45.x, ut, ws);
-    double wt = mul_rn(g23.x, ur);
+    T wt = mul_rn(g23.x, ur);
     wt = fma_rn(g45.x, us, wt);
     wt = fma_rn(g45.y, ut, wt);
     sm.B[q] = wr;
@@ -873,43 +888,43 @@ __global__ void __launch_bounds__(LX * LX)
   // transposed gradient (local_grad3_t, cg.f:189-212) with D^T
   {
     const int l0 = t % LX, l1 = t / LX;
-    double v[LX], y[LX];
+    T v[LX], y[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<LX>(m, l0, l1)];  // wr line (j,k)
-    eo_line<LX>(v, Et, Ot, y);
+    eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
     for (int m = 0; m < LX; ++m) sm.A[eo_at<LX>(m, l0, l1)] = y[m];  // tr
   }
   __syncthreads();
   {
     const int l0 = t % LX, l1 = t / LX;
-    double v[LX], y[LX];
+    T v[LX], y[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<LX>(l0, m, l1)];  // ws line (i,k)
-    eo_line<LX>(v, Et, Ot, y);
+    eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
     for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(l0, m, l1)] = y[m];  // ts
   }
-  double ttreg[LX];
-  eo_line<LX>(wtreg, Et, Ot, ttreg);
+  T ttreg[LX];
+  eo_line<T, LX>(wtreg, Et, Ot, ttreg);
   __syncthreads();
 
-  double part = 0.0;
+  T part = T(0);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = eo_at<LX>(i, j, k);
-    double wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
+    T wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
     const size_t id = base + size_t(k) * L2 + t;
     const bool interior = col_interior && (k > 0) && (k < LX - 1);
     if (MODE == 1) {
       if (interior) {
-        wl = fma_rn(0.1, ureg[k], wl);
+        wl = fma_rn(T(0.1), ureg[k], wl);
         part = fma_rn(mul_rn(wl, creg[k]), ureg[k], part);
       }
       a.w[id] = wl;
     } else if (MODE == 2) {
       if (interior) {
-        const double rv = freg[k] - fma_rn(0.1, ureg[k], wl);
+        const T rv = freg[k] - fma_rn(T(0.1), ureg[k], wl);
         a.r[id] = rv;
         part = fma_rn(mul_rn(rv, creg[k]), rv, part);
       } else {
@@ -920,14 +935,14 @@ __global__ void __launch_bounds__(LX * LX)
     }
   }
   if (MODE != 0) {
-    const double s = block_sum<double>(part, sm.red);
+    const double s = block_sum<T>(part, sm.red);
     if (t == 0) a.partial[e] = s;
   }
 }
 
-template <int LX>
+template <typename T, int LX, bool TMAG>
 constexpr size_t ax_eo_smem_bytes() {
-  return sizeof(AxEoShared<LX>);
+  return sizeof(AxEoShared<T, LX, TMAG>);
 }
 
 }  // namespace nb

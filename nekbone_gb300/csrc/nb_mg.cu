@@ -612,6 +612,7 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
       at(2, 2, 1, e) = lm;
       at(2, 2, lx, e) = lm;
     }
+    NB_TRY(ensure_host_maps(const_cast<Operator &>(op)));
     gs_host_add(op.gsh_host, lw.data());
     for (int l = 2; l <= nlev; ++l) {
       MgLevel &L = mg->lv[l];

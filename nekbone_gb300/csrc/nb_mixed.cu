@@ -153,10 +153,9 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
   cudaStream_t s = lib_stream();
   const long n = op.n;
   if (check_every < 1) check_every = 1;
-  double *r, *w, *p;
-  NB_CUDA(cudaMalloc(&r, n * 8));
-  NB_CUDA(cudaMalloc(&w, n * 8));
-  NB_CUDA(cudaMalloc(&p, n * 8));
+  NB_TRY(wk.ensure_scratch(size_t(3) * n * 8));
+  double *r = reinterpret_cast<double *>(wk.scratch);
+  double *w = r + n, *p = w + n;
   int done = 0;
   double rn0 = 0, rn = 0;
   // run CG in chunks: cg_device always starts from x=0, so iterate one long
@@ -175,9 +174,6 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
       if (rn0 > 0 && rn / rn0 <= tol) break;
     }
   }
-  cudaFree(r);
-  cudaFree(w);
-  cudaFree(p);
   if (st) return st;
   if (iters) *iters = done;
   if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
@@ -194,23 +190,14 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   CgWork &wk = *static_cast<CgWork *>(pwk);
   cudaStream_t s = lib_stream();
   const long n = op.n;
-  double *r = nullptr, *w = nullptr;
-  float *g32 = nullptr, *c32 = nullptr, *r32 = nullptr, *e32 = nullptr,
-        *rr32 = nullptr, *w32 = nullptr, *p32 = nullptr;
-  int st = NB_OK;
-  auto A = [&](void **p, size_t b) {
-    if (st) return;
-    if (cudaMalloc(p, b) != cudaSuccess) st = fail(NB_ERR_CUDA, "nb_cg_mixed: out of memory");
-  };
-  A((void **)&r, n * 8);
-  A((void **)&w, n * 8);
-  A((void **)&g32, 6 * n * 4);
-  A((void **)&c32, n * 4);
-  A((void **)&r32, n * 4);
-  A((void **)&e32, n * 4);
-  A((void **)&rr32, n * 4);
-  A((void **)&w32, n * 4);
-  A((void **)&p32, n * 4);
+  // scratch: r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32 (FP32)
+  int st = wk.ensure_scratch(size_t(n) * (2 * 8 + 12 * 4));
+  if (st) return st;
+  double *r = reinterpret_cast<double *>(wk.scratch);
+  double *w = r + n;
+  float *g32 = reinterpret_cast<float *>(w + n);
+  float *c32 = g32 + 6 * n, *r32 = c32 + n, *e32 = r32 + n, *rr32 = e32 + n,
+        *w32 = rr32 + n, *p32 = w32 + n;
   int k = 0, inner = 0;
   double rn0 = 0.0, rn = 0.0;
   if (!st) st = vec_convert<float, double>(g32, g, 6 * n, s);
@@ -249,8 +236,6 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     inner += inner_iters;
     ++k;
   }
-  cudaFree(r); cudaFree(w); cudaFree(g32); cudaFree(c32); cudaFree(r32);
-  cudaFree(e32); cudaFree(rr32); cudaFree(w32); cudaFree(p32);
   if (st) return st;
   if (outer) *outer = k;
   if (inner_total) *inner_total = inner;

@@ -21,6 +21,7 @@ namespace nb {
 
 Operator::~Operator() {
   if (dEO) cudaFree(dEO);
+  if (fEO) cudaFree(fEO);
   if (dD) cudaFree(dD);
   if (fD) cudaFree(fD);
   gs_release(&gs);
@@ -36,6 +37,18 @@ CgWork::~CgWork() {
     if (p) cudaFree(p);
   if (counters) cudaFree(counters);
   if (sc) cudaFree(sc);
+  if (scratch) cudaFree(scratch);
+}
+
+int CgWork::ensure_scratch(size_t bytes) {
+  if (bytes <= scratch_bytes) return NB_OK;
+  if (scratch) cudaFree(scratch);
+  scratch = nullptr;
+  scratch_bytes = 0;
+  if (cudaMalloc(&scratch, bytes) != cudaSuccess)
+    return fail(NB_ERR_CUDA, "solver scratch: out of device memory (%zu bytes)", bytes);
+  scratch_bytes = bytes;
+  return NB_OK;
 }
 
 static int sm_count() {
@@ -192,9 +205,8 @@ int operator_set_mask(Operator *op, const std::vector<int> &list_in) {
   return NB_OK;
 }
 
-int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
-                  const int *lglel, const double *dxm1, const GsHost &maps,
-                  int mask_mode, cudaStream_t s) {
+int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
+                  const int *lglel, const double *dxm1, int mask_mode, cudaStream_t s) {
   if (lx < 2 || lx > kMaxLx)
     return fail(NB_ERR_UNSUPPORTED, "lx1=%d outside the supported range 2..%d", lx, kMaxLx);
   if (nelt <= 0) return fail(NB_ERR_ARG, "nelt=%d must be positive", nelt);
@@ -235,16 +247,27 @@ int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
       NB_CUDA(cudaMalloc(&op->dEO, eo.size() * sizeof(double)));
       NB_CUDA(cudaMemcpy(op->dEO, eo.data(), eo.size() * sizeof(double),
                          cudaMemcpyHostToDevice));
+      std::vector<float> eo32(eo.begin(), eo.end());
+      NB_CUDA(cudaMalloc(&op->fEO, eo32.size() * sizeof(float)));
+      NB_CUDA(cudaMemcpy(op->fEO, eo32.data(), eo32.size() * sizeof(float),
+                         cudaMemcpyHostToDevice));
       op->eo_ok = true;
     }
   }
-  op->gsh_host = maps;
-  NB_TRY(gs_upload(op->gsh_host, int(op->n), &op->gs, s));
   op->face.resize(nelt);
   for (int e = 0; e < nelt; ++e)
     op->face[e] = (unsigned char)face_bits(op->lglel[e], nelx, nely, nelz);
   NB_CUDA(cudaMalloc(&op->d_face, nelt));
   NB_CUDA(cudaMemcpy(op->d_face, op->face.data(), nelt, cudaMemcpyHostToDevice));
+  return NB_OK;
+}
+
+int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
+                  const int *lglel, const double *dxm1, const GsHost &maps,
+                  int mask_mode, cudaStream_t s) {
+  NB_TRY(operator_base(op, nelx, nely, nelz, nelt, lx, lglel, dxm1, mask_mode, s));
+  op->gsh_host = maps;
+  NB_TRY(gs_upload(op->gsh_host, int(op->n), &op->gs, s));
   build_boundary_groups(op);
   op->mask_built = false;
   if (mask_mode == 1) {
@@ -268,6 +291,11 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
   for (long e = 0; e < nelt; ++e) lglel[e] = int(e + 1);  // brick, np=1
   std::vector<double> a(lx * lx), b(lx), c(lx * lx), d(lx * lx), z(lx);
   semhat(a.data(), b.data(), c.data(), d.data(), z.data(), lx - 1);
+  if (mask_mode == 1 && setup_on_device()) {
+    NB_TRY(operator_base(op, nelx, nely, nelz, int(nelt), lx, lglel.data(), d.data(),
+                         mask_mode, s));
+    return box_topology_device(op, s);
+  }
   const long n = nelt * lx * lx * lx;
   std::vector<int64_t> glo(n);
   set_vert_box(glo.data(), lx, int(nelt), nelx, nely, lglel.data());
@@ -275,6 +303,14 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
   gs_topology(glo.data(), int(n), &maps);
   return operator_from(op, nelx, nely, nelz, int(nelt), lx, lglel.data(),
                        d.data(), maps, mask_mode, s);
+}
+
+int ensure_host_maps(Operator &op) {
+  if (!op.gsh_host.map[0].empty()) return NB_OK;
+  std::vector<int64_t> glo(op.n);
+  set_vert_box(glo.data(), op.lx, op.nelt, op.nelx, op.nely, op.lglel.data());
+  gs_topology(glo.data(), int(op.n), &op.gsh_host);
+  return NB_OK;
 }
 
 // ------------------------------------------------------- vector kernels --

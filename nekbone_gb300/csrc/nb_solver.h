@@ -21,8 +21,10 @@ struct Operator {
   // even-odd split of D (E, O of D and of D^T, 4*(lx/2)^2); valid when lx is
   // even and D is anti-centrosymmetric to rounding
   double *dEO = nullptr;
+  float *fEO = nullptr;            // the same tables in FP32
   bool eo_ok = false;
   int order = 1;                   // 0 reference left-to-right sums, 1 even-odd
+                                   // (FP64 and FP32 operators alike)
   GsHost gsh_host;                 // jl maps of the dssum handle
   GsDevice gs;                     // device form
   // mask state (maskit, cg.f:214-258)
@@ -55,8 +57,13 @@ struct CgWork {
   int hist_len = 0;
   double *dot_out = nullptr;
   int grid_up = 0, grid_gs = 0, cap_ax = 0;
+  // vector scratch of the solvers to a tolerance (kept between calls, so a
+  // repeated solve allocates nothing)
+  unsigned char *scratch = nullptr;
+  size_t scratch_bytes = 0;
   ~CgWork();
   int ensure(const Operator &op, int niter);
+  int ensure_scratch(size_t bytes);
 };
 
 // Builds the operator for a box of nelx*nely*nelz elements with lx points
@@ -68,6 +75,20 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
 int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt,
                   int lx, const int *lglel, const double *dxm1,
                   const GsHost &maps, int mask_mode, cudaStream_t s);
+// The mesh-independent part of an operator: sizes, element numbers, D and
+// its even-odd tables, the domain faces of every element.
+int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
+                  const int *lglel, const double *dxm1, int mask_mode, cudaStream_t s);
+// The gather-scatter groups, the fused boundary groups with their mask flags
+// and the full Dirichlet mask list of a brick-ordered box, built on the
+// device without a sort (nb_topo.cu).  The host jl maps stay empty until
+// ensure_host_maps builds them.
+int box_topology_device(Operator *op, cudaStream_t s);
+int ensure_host_maps(Operator &op);
+// Whether operator_box builds full-mask topologies on the device (default
+// on); the host path (jl's sort-based construction) stays available.
+bool setup_on_device();
+void set_setup_on_device(bool on);
 // Re-derives the device mask list and the fused-path mask flags.
 int operator_set_mask(Operator *op, const std::vector<int> &list);
 // Full Dirichlet mask of every element's domain faces (get_face per element).
