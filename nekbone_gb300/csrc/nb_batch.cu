@@ -35,6 +35,7 @@
 
 #include "../../include/nekbone_gb300.h"
 #include "nb_batch.h"
+#include "nb_solver.h"
 
 namespace nb {
 
@@ -431,8 +432,8 @@ struct Batch {
   struct Group {
     int lx = 0, el0 = 0, nel = 0;
     long pt0 = 0, n = 0;
-    double *D64 = nullptr;
-    float *D32 = nullptr;
+    double *D64 = nullptr, *EO64 = nullptr;
+    float *D32 = nullptr, *EO32 = nullptr;
     BatchTune tune;
   };
   int nprob = 0;
@@ -469,6 +470,8 @@ struct Batch {
     for (auto &G : groups) {
       cudaFree(G.D64);
       cudaFree(G.D32);
+      if (G.EO64) cudaFree(G.EO64);
+      if (G.EO32) cudaFree(G.EO32);
     }
     void *ptrs[] = {x, f, g, c, r, w, g32, c32, r32, e32, p32, w32, el_prob, off, gch_g0,
                     gch_prob, pch_prob, cycles, idx, cnt, pch_q0, pb, sc, part_ax, part_gs,
@@ -486,6 +489,7 @@ struct Batch {
       a.g = g32;
       a.c = c32;
       a.D = G.D32;
+      a.eo = G.EO32;
       a.el_prob = el_prob;
       a.sc = sc;
       a.partial = part_ax;
@@ -505,6 +509,7 @@ struct Batch {
       a.g = g;
       a.c = c;
       a.D = G.D64;
+      a.eo = G.EO64;
       a.f = f;
       a.r = r;
       a.e = e32;
@@ -778,12 +783,17 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
     std::vector<float> d32(d.begin(), d.end());
     NB_TRY(upload(&G.D64, d));
     NB_TRY(upload(&G.D32, d32));
-    // default shape: the single-mesh operator's (one element per block,
-    // register D for FP32) where instantiated, else the smallest count
+    std::vector<double> eo;
+    if (even_odd_tables(d, L, eo)) {
+      std::vector<float> eo32(eo.begin(), eo.end());
+      NB_TRY(upload(&G.EO64, eo));
+      NB_TRY(upload(&G.EO32, eo32));
+    }
+    // default shape: the first listed (the even-odd form where lx1 is even)
     const auto s32 = batch_shapes_f32(L);
     const auto s64 = batch_shapes_f64(L);
     G.tune.epb32 = s32.front().first;
-    G.tune.rd32 = 1;
+    G.tune.rd32 = s32.front().second;
     G.tune.epb64 = s64.front();
   }
   return NB_OK;
@@ -798,23 +808,24 @@ std::vector<std::pair<int, int>> batch_shapes_f32(int lx) {
     case 6: e = {2, 4, 8}; break;
     default: e = {1, 2, 4}; break;
   }
+  // the even-odd form first (even lx1), then register D, then shared D,
+  // smallest element count first
   std::vector<std::pair<int, int>> out;
+  if (lx % 2 == 0) out.push_back({1, 2});
   for (int rd = 1; rd >= 0; --rd)
     for (int v : e) out.push_back({v, rd});
-  // order: register-D shapes first, smallest element count first
-  std::stable_sort(out.begin(), out.end(), [](const std::pair<int, int> &a,
-                                               const std::pair<int, int> &b) {
-    return a.second > b.second;
-  });
   return out;
 }
 
 std::vector<int> batch_shapes_f64(int lx) {
+  std::vector<int> out;
+  if (lx % 2 == 0) out.push_back(0);   // even-odd form
   switch (lx) {
-    case 4: return {4, 8};
-    case 6: return {2, 4};
-    default: return {1, 2};
+    case 4: out.insert(out.end(), {4, 8}); break;
+    case 6: out.insert(out.end(), {2, 4}); break;
+    default: out.insert(out.end(), {1, 2}); break;
   }
+  return out;
 }
 
 }  // namespace nb
@@ -921,13 +932,13 @@ int nb_batch_set_tuning(nb_batch *b, int lx1, int epb32, int rd32, int epb64) {
   for (auto &G : b->B.groups)
     if (G.lx == lx1) {
       bool ok32 = false, ok64 = false;
-      for (auto sh : batch_shapes_f32(lx1)) ok32 |= sh.first == epb32 && sh.second == (rd32 != 0);
+      for (auto sh : batch_shapes_f32(lx1)) ok32 |= sh.first == epb32 && sh.second == rd32;
       for (int v : batch_shapes_f64(lx1)) ok64 |= v == epb64;
       if (!ok32 || !ok64)
         return fail(NB_ERR_UNSUPPORTED, "nb_batch_set_tuning: shape not instantiated for lx1=%d",
                     lx1);
       G.tune.epb32 = epb32;
-      G.tune.rd32 = rd32 != 0;
+      G.tune.rd32 = rd32;
       G.tune.epb64 = epb64;
       if (b->B.exec) {
         cudaGraphExecDestroy(b->B.exec);
@@ -986,6 +997,7 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.g = B.g32;
       a.c = B.c32;
       a.D = G.D32;
+      a.eo = G.EO32;
       a.el_prob = B.el_prob;
       a.sc = B.sc;
       a.partial = B.part_ax;
@@ -1018,6 +1030,7 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.g = B.g;
       a.c = B.c;
       a.D = G.D64;
+      a.eo = G.EO64;
       a.f = B.f;
       a.r = B.r;
       a.e = B.e32;

@@ -36,8 +36,9 @@ struct BatchProb {
 // Launch shape of the batched element operator for one lx1.
 struct BatchTune {
   int epb32 = 1;    // elements per block, FP32 inner operator
-  int rd32 = 1;     // 1: D in registers + vector shared loads; 0: padded shared D
-  int epb64 = 1;    // elements per block, FP64 defect operator
+  int rd32 = 1;     // 1: D in registers + vector shared loads; 0: padded shared D;
+                    // 2: even-odd, one 1-D line per thread (epb 1)
+  int epb64 = 1;    // elements per block, FP64 defect operator (0: even-odd form)
   float ms32 = 0.f, ms64 = 0.f;  // measured time of the chosen shapes
 };
 
@@ -56,6 +57,7 @@ struct BaxArgs {
   const T *f;          // MODE 2
   T *r;                // MODE 2
   const float *e;      // MODE 2: FP32 correction
+  const T *eo;         // even-odd tables of D (forms with epb 0 / rd 2)
   const int *el_prob;  // element -> problem
   const BatchScalars *sc;
   double *partial;     // per element

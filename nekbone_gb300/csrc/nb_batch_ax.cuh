@@ -231,6 +231,181 @@ __global__ void __launch_bounds__(LX * LX * EPB)
   }
 }
 
+// The even-odd form for the batch: one element per CTA, one 1-D line per
+// thread in each contraction (the single-mesh k_ax_eo), with the per-element
+// problem lookups of k_bax.  TMAG: the element's metric block arrives by one
+// bulk copy (FP32).
+template <typename T, int LX, int MODE, bool TMAG>
+__global__ void __launch_bounds__(LX * LX)
+    k_bax_eo(BaxArgs<T> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  AxEoShared<T, LX, TMAG> &sm = *reinterpret_cast<AxEoShared<T, LX, TMAG> *>(smem_raw);
+  constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
+  const int t = threadIdx.x + LX * threadIdx.y;
+  const int i = threadIdx.x, j = threadIdx.y;
+  const int e = a.el0 + blockIdx.x;
+  const int prob = a.el_prob[e];
+  if (!a.sc[prob].active) return;   // the whole CTA: one element
+  const size_t base = size_t(a.pt0) + size_t(blockIdx.x) * L3;
+  if (TMAG && t == 0) {
+    constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));
+    mbar_init(&sm.bar, 1);
+    mbar_arrive_expect_tx(&sm.bar, GBYTES);
+    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
+  }
+  const T *Ed = sm.E4, *Od = sm.E4 + H * H;
+  const T *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;
+  for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = a.eo[q];
+
+  const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
+  T creg[LX], freg[LX];
+  if (col_interior) {
+#pragma unroll
+    for (int k = 1; k < LX - 1; ++k) {
+      const size_t id = base + size_t(k) * L2 + t;
+      creg[k] = a.c[id];
+      if (MODE == 2) freg[k] = a.f[id];
+    }
+  }
+  T ureg[LX], pold[LX];
+  const T beta = (MODE == 1 && !a.first) ? T(a.sc[prob].beta) : T(0);
+  const T scale = MODE == 2 ? T(a.sc[prob].rn) : T(0);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + t;
+    if (MODE == 1) {
+      ureg[k] = a.u[id];
+      pold[k] = a.first ? T(0) : a.p[id];
+    } else {
+      ureg[k] = a.p[id];
+      pold[k] = T(a.e[id]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const size_t id = base + size_t(k) * L2 + t;
+    if (MODE == 1) {
+      if (!a.first) ureg[k] = fma_rn(beta, pold[k], ureg[k]);
+    } else {
+      ureg[k] = fma_rn(scale, pold[k], ureg[k]);
+    }
+    a.p[id] = ureg[k];
+    sm.A[eo_at<LX>(i, j, k)] = ureg[k];
+  }
+  __syncthreads();
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    T v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(m, l0, l1)];
+    eo_line<T, LX>(v, Ed, Od, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(m, l0, l1)] = y[m];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(l0, m, l1)];
+    eo_line<T, LX>(v, Ed, Od, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.C[eo_at<LX>(l0, m, l1)] = y[m];
+  }
+  T wtreg[LX];
+  eo_line<T, LX>(ureg, Ed, Od, wtreg);
+  __syncthreads();
+  if (TMAG) mbar_wait_bounded(&sm.bar, 0, nullptr);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = eo_at<LX>(i, j, k);
+    const T ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
+    const size_t pt = base + size_t(k) * L2 + t;
+    typedef typename Vec2<T>::type V2;
+    const V2 *gp = TMAG ? reinterpret_cast<const V2 *>(&sm.g[6 * (k * L2 + t)])
+                        : reinterpret_cast<const V2 *>(a.g + 6 * pt);
+    const V2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
+    T wr = mul_rn(g01.x, ur);
+    wr = fma_rn(g01.y, us, wr);
+    wr = fma_rn(g23.x, ut, wr);
+    T ws = mul_rn(g01.y, ur);
+    ws = fma_rn(g23.y, us, ws);
+    ws = fma_rn(g45.x, ut, ws);
+    T wt = mul_rn(g23.x, ur);
+    wt = fma_rn(g45.x, us, wt);
+    wt = fma_rn(g45.y, ut, wt);
+    sm.B[q] = wr;
+    sm.C[q] = ws;
+    wtreg[k] = wt;
+  }
+  __syncthreads();
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    T v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<LX>(m, l0, l1)];
+    eo_line<T, LX>(v, Et, Ot, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.A[eo_at<LX>(m, l0, l1)] = y[m];
+  }
+  __syncthreads();
+  {
+    const int l0 = t % LX, l1 = t / LX;
+    T v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<LX>(l0, m, l1)];
+    eo_line<T, LX>(v, Et, Ot, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(l0, m, l1)] = y[m];
+  }
+  T ttreg[LX];
+  eo_line<T, LX>(wtreg, Et, Ot, ttreg);
+  __syncthreads();
+  T part = T(0);
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = eo_at<LX>(i, j, k);
+    T wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
+    const size_t id = base + size_t(k) * L2 + t;
+    const bool interior = col_interior && (k > 0) && (k < LX - 1);
+    if (MODE == 1) {
+      if (interior) {
+        wl = fma_rn(T(0.1), ureg[k], wl);
+        part = fma_rn(mul_rn(wl, creg[k]), ureg[k], part);
+      }
+      a.w[id] = wl;
+    } else {
+      if (interior) {
+        const T rv = freg[k] - fma_rn(T(0.1), ureg[k], wl);
+        a.r[id] = rv;
+        part = fma_rn(mul_rn(rv, creg[k]), rv, part);
+      } else {
+        a.w[id] = wl;
+      }
+    }
+  }
+  const double s = block_sum<T>(part, sm.red);
+  if (t == 0) a.partial[e] = s;
+}
+
+template <typename T, int LX, int MODE>
+int launch_bax_eo(const BaxArgs<T> &a, cudaStream_t s) {
+  if constexpr (LX % 2 != 0) {
+    return fail(NB_ERR_UNSUPPORTED, "batched even-odd operator: odd lx1=%d", LX);
+  } else {
+    constexpr bool TMAG = sizeof(T) == 4;   // element metric blocks are 16-byte aligned
+    const size_t smem = sizeof(AxEoShared<T, LX, TMAG>);
+    static bool attr = false;
+    if (!attr) {
+      NB_CUDA(cudaFuncSetAttribute(k_bax_eo<T, LX, MODE, TMAG>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+      attr = true;
+    }
+    if (a.nel <= 0) return NB_OK;
+    if (!a.eo) return fail(NB_ERR_STATE, "batched even-odd operator: no tables");
+    if (TMAG && (reinterpret_cast<uintptr_t>(a.g + 6 * a.pt0) & 15u))
+      return fail(NB_ERR_STATE, "batched even-odd operator: metric not 16-byte aligned");
+    k_bax_eo<T, LX, MODE, TMAG><<<a.nel, dim3(LX, LX), smem, s>>>(a);
+    NB_CUDA(cudaGetLastError());
+    return NB_OK;
+  }
+}
+
 template <typename T, int LX, int MODE, bool RD, int EPB>
 int launch_bax(const BaxArgs<T> &a, cudaStream_t s) {
   const size_t smem = sizeof(BaxShared<T, LX, EPB>);
@@ -260,7 +435,9 @@ template <> struct BaxEpb<12> { static constexpr int a = 1, b = 2, c = 4; };
 template <int LX>
 int batch_ax_f32_lx(int epb, int rd, const BaxArgs<float> &a, cudaStream_t s) {
   typedef BaxEpb<LX> P;
-  if (rd) {
+  if (rd == 2) {
+    if (epb == 1) return launch_bax_eo<float, LX, 1>(a, s);
+  } else if (rd) {
     if (epb == P::a) return launch_bax<float, LX, 1, true, P::a>(a, s);
     if (epb == P::b) return launch_bax<float, LX, 1, true, P::b>(a, s);
     if (epb == P::c) return launch_bax<float, LX, 1, true, P::c>(a, s);
@@ -276,6 +453,7 @@ int batch_ax_f32_lx(int epb, int rd, const BaxArgs<float> &a, cudaStream_t s) {
 template <int LX>
 int batch_ax_f64_lx(int epb, const BaxArgs<double> &a, cudaStream_t s) {
   typedef BaxEpb<LX> P;
+  if (epb == 0) return launch_bax_eo<double, LX, 2>(a, s);   // even-odd form
   if (epb == P::a) return launch_bax<double, LX, 2, false, P::a>(a, s);
   if (epb == P::b) return launch_bax<double, LX, 2, false, P::b>(a, s);
   return fail(NB_ERR_UNSUPPORTED, "batched FP64 operator: no shape epb=%d for lx1=%d", epb, LX);

@@ -97,6 +97,28 @@ int CgWork::ensure(const Operator &op, int niter) {
 }
 
 // ------------------------------------------------------------ set-up --
+bool even_odd_tables(const std::vector<double> &D, int lx, std::vector<double> &eo) {
+  if (lx % 2 != 0) return false;
+  double dmax = 0.0, asym = 0.0;
+  auto Dm = [&](int r, int c) { return D[r + c * lx]; };
+  for (int r = 0; r < lx; ++r)
+    for (int c = 0; c < lx; ++c) {
+      dmax = std::max(dmax, std::fabs(Dm(r, c)));
+      asym = std::max(asym, std::fabs(Dm(r, c) + Dm(lx - 1 - r, lx - 1 - c)));
+    }
+  if (asym > 1e-12 * dmax) return false;
+  const int h = lx / 2;
+  eo.assign(4 * h * h, 0.0);
+  for (int a = 0; a < h; ++a)
+    for (int m = 0; m < h; ++m) {
+      eo[a * h + m] = (Dm(a, m) + Dm(a, lx - 1 - m)) / 2;
+      eo[h * h + a * h + m] = (Dm(a, m) - Dm(a, lx - 1 - m)) / 2;
+      eo[2 * h * h + a * h + m] = (Dm(m, a) + Dm(lx - 1 - m, a)) / 2;
+      eo[3 * h * h + a * h + m] = (Dm(m, a) - Dm(lx - 1 - m, a)) / 2;
+    }
+  return true;
+}
+
 static bool is_elem_boundary(long pt, int lx) {
   const long l3 = long(lx) * lx * lx;
   const int r = int(pt % l3);
@@ -226,24 +248,9 @@ int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
   NB_CUDA(cudaMemcpy(op->dD, op->D.data(), lx * lx * sizeof(double), cudaMemcpyHostToDevice));
   NB_CUDA(cudaMemcpy(op->fD, fDh.data(), lx * lx * sizeof(float), cudaMemcpyHostToDevice));
   // even-odd tables when D(n-1-i,n-1-m) = -D(i,m) holds to rounding
-  if (lx % 2 == 0) {
-    double dmax = 0.0, asym = 0.0;
-    auto Dm = [&](int r, int c) { return op->D[r + c * lx]; };
-    for (int r = 0; r < lx; ++r)
-      for (int c = 0; c < lx; ++c) {
-        dmax = std::max(dmax, std::fabs(Dm(r, c)));
-        asym = std::max(asym, std::fabs(Dm(r, c) + Dm(lx - 1 - r, lx - 1 - c)));
-      }
-    if (asym <= 1e-12 * dmax) {
-      const int h = lx / 2;
-      std::vector<double> eo(4 * h * h);
-      for (int a = 0; a < h; ++a)
-        for (int m = 0; m < h; ++m) {
-          eo[a * h + m] = (Dm(a, m) + Dm(a, lx - 1 - m)) / 2;
-          eo[h * h + a * h + m] = (Dm(a, m) - Dm(a, lx - 1 - m)) / 2;
-          eo[2 * h * h + a * h + m] = (Dm(m, a) + Dm(lx - 1 - m, a)) / 2;
-          eo[3 * h * h + a * h + m] = (Dm(m, a) - Dm(lx - 1 - m, a)) / 2;
-        }
+  {
+    std::vector<double> eo;
+    if (even_odd_tables(op->D, lx, eo)) {
       NB_CUDA(cudaMalloc(&op->dEO, eo.size() * sizeof(double)));
       NB_CUDA(cudaMemcpy(op->dEO, eo.data(), eo.size() * sizeof(double),
                          cudaMemcpyHostToDevice));

@@ -75,6 +75,9 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
 int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt,
                   int lx, const int *lglel, const double *dxm1,
                   const GsHost &maps, int mask_mode, cudaStream_t s);
+// E, O of D and of D^T (4*(lx/2)^2 values) when lx is even and D is
+// anti-centrosymmetric to rounding (the even-odd contraction form).
+bool even_odd_tables(const std::vector<double> &D, int lx, std::vector<double> &eo);
 // The mesh-independent part of an operator: sizes, element numbers, D and
 // its even-odd tables, the domain faces of every element.
 int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,

@@ -189,3 +189,27 @@ def test_host_copies_round_trip(torch):
     for p in range(2):
         assert b.result(p)[2] <= 1e-10
     b.close()
+
+
+def test_even_odd_forms_agree(torch):
+    """The even-odd forms (one line per thread; FP32 metric by bulk copy)
+    sum in a different order: same tolerance met, solutions within 1e-8."""
+    import nekbone_gb300 as nb
+    boxes = [(2, 2, 1, 4), (2, 1, 2, 6), (1, 2, 2, 8), (2, 1, 1, 10), (1, 1, 2, 12)]
+    b = nb.Batch(boxes)
+    b.setup(3)
+    xs = []
+    for eo in (False, True):
+        for lx in (4, 6, 8, 10, 12):
+            if eo:
+                b.set_tuning(lx, 1, 2, 0)
+            else:
+                b.set_tuning(lx, 4 if lx == 4 else (2 if lx == 6 else 1), 1,
+                             4 if lx == 4 else (2 if lx == 6 else 1))
+        b.solve(1e-10, 20, 40)
+        nb.sync()
+        xs.append(_view(torch, b.arrays()[0], b.n).cpu().numpy().copy())
+        for p in range(len(boxes)):
+            assert b.result(p)[2] <= 1e-10
+    assert np.max(np.abs(xs[0] - xs[1])) <= 1e-8 * np.max(np.abs(xs[0]))
+    b.close()
