@@ -66,6 +66,11 @@ void nekbone_set_contraction_order_(const int *order);
 void nekbone_get_flops_(double *flop_a, double *flop_cg);
 void nekbone_set_flops_(const double *flop_a, const double *flop_cg);
 
+/* What the last cg_ would print (cg.f:44,79): *iter = niter+1, rnorm at
+ * iteration 0 and at the end, and the last alpha, beta and pap. */
+void nekbone_cg_report_(int *iter, double *rnorm0, double *rnorm, double *alpha,
+                        double *beta, double *pap);
+
 /* --------------------------------------- jl gather-scatter (jl/gs.c) -- */
 /* gs_setup_ (jl/gs.c:1160-1170).  comm/np are accepted for signature
  * compatibility; one process (np == 1) is supported. */

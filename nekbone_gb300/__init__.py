@@ -54,7 +54,7 @@ EXPORTS = (
     "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_mesh_gs_maps",
-    "nb_mesh_boundary_groups", "nb_mesh_mask_list",
+    "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
 )
 
 lib.nekbone_last_status.restype = _i

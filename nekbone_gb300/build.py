@@ -83,7 +83,28 @@ def build(force: bool = False, jobs: int | None = None, verbose: bool = False) -
         if p.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
         os.replace(tmp, LIB)
+    build_driver(force)
     return LIB
+
+
+DRIVER_SRC = PKG / "driver" / "nekbone.cpp"
+DRIVER = PKG / "bin" / "nekbone"
+
+
+def build_driver(force: bool = False) -> Path:
+    """The reference's driver program over the C ABI (host C++ only)."""
+    DRIVER.parent.mkdir(exist_ok=True)
+    if (not force and DRIVER.exists() and DRIVER.stat().st_mtime >= LIB.stat().st_mtime
+            and DRIVER.stat().st_mtime >= DRIVER_SRC.stat().st_mtime):
+        return DRIVER
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", str(ROOT / "include"),
+           "-o", str(DRIVER), str(DRIVER_SRC), "-L", str(PKG), "-lnekbone_gb300",
+           "-Wl,-rpath,$ORIGIN/.."]
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{p.stdout}\n{p.stderr}")
+    return DRIVER
 
 
 def main() -> None:

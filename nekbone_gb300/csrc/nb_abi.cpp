@@ -599,6 +599,43 @@ void cg_(double *x, const double *f, const double *g, const double *c,
   S.flop_cg = *flop_cg;
 }
 
+// The values the reference's cg prints (cg.f:44,79): rnorm at iteration 0,
+// then the final iteration count (niter+1), rnorm, alpha, beta, pap.
+void nekbone_cg_report_(int *iter, double *rnorm0, double *rnorm, double *alpha,
+                        double *beta, double *pap) {
+  clear_status();
+  State &S = st();
+  if (!S.wk.sc) {
+    fail(NB_ERR_STATE, "nekbone_cg_report: no cg call yet");
+    return;
+  }
+  CgScalars sc;
+  if (cudaMemcpyAsync(&sc, S.wk.sc, sizeof(sc), cudaMemcpyDeviceToHost, S.s) != cudaSuccess ||
+      cudaStreamSynchronize(S.s) != cudaSuccess) {
+    fail(NB_ERR_CUDA, "nekbone_cg_report: reading the solver scalars");
+    return;
+  }
+  // the history rows (rnorm, alpha, beta, pap, rtz1) of iteration 0 and of
+  // the last iteration: the scalars themselves already hold the next beta
+  double h0[5] = {0, 0, 0, 0, 0}, hl[5] = {sc.rnorm, sc.alpha, sc.beta, sc.pap, sc.rtz1};
+  if (S.wk.hist && sc.iter < S.wk.hist_len) {
+    if (cudaMemcpyAsync(h0, S.wk.hist, sizeof(h0), cudaMemcpyDeviceToHost, S.s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(hl, S.wk.hist + 5 * sc.iter, sizeof(hl), cudaMemcpyDeviceToHost,
+                        S.s) != cudaSuccess ||
+        cudaStreamSynchronize(S.s) != cudaSuccess) {
+      fail(NB_ERR_CUDA, "nekbone_cg_report: reading the iteration history");
+      return;
+    }
+  }
+  if (iter) *iter = sc.iter + 1;
+  if (rnorm0) *rnorm0 = h0[0];
+  if (rnorm) *rnorm = hl[0];
+  if (alpha) *alpha = hl[1];
+  if (beta) *beta = hl[2];
+  if (pap) *pap = hl[3];
+}
+
 // -------------------------------------------------------------- hsmg.f --
 void h1mg_setup_(void) {
   clear_status();
