@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <tuple>
 
 #include "nb_mg.h"
 
@@ -558,10 +560,17 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
     zh[l].resize(nh);
     std::vector<double> c(nh * nh), d(nh * nh);
     semhat(ah[l].data(), bh[l].data(), c.data(), d.data(), zh[l].data(), ord[l]);
-    L.gs_host = numbering(op, nh);
-    L.gsx_host = numbering(op, nh + 2);
-    NB_TRY(gs_upload(L.gs_host, int(L.n), &L.gs, s));
-    NB_TRY(gs_upload(L.gsx_host, int(L.next), &L.gsx, s));
+    if (op.brick && setup_on_device()) {
+      // box numberings of nh and nh+2 points per direction (set_vert_box
+      // through proxy_setupds, hsmg.f:161-166), built on the device
+      NB_TRY(box_gs_device(nh, op.nelx, op.nely, op.nelz, &L.gs, s));
+      NB_TRY(box_gs_device(nh + 2, op.nelx, op.nely, op.nelz, &L.gsx, s));
+    } else {
+      L.gs_host = numbering(op, nh);
+      L.gsx_host = numbering(op, nh + 2);
+      NB_TRY(gs_upload(L.gs_host, int(L.n), &L.gs, s));
+      NB_TRY(gs_upload(L.gsx_host, int(L.next), &L.gsx, s));
+    }
     NB_TRY(dmalloc(&L.e, L.n));
     NB_TRY(dmalloc(&L.r, L.n));
     const std::vector<int> mk = level_mask(op, nh);
@@ -619,18 +628,40 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
       const int nl = L.nl, n = L.order;
       std::vector<double> S(size_t(nl) * nl * 6 * nelt), Dd(size_t(nl) * nl * nl * nelt);
       std::vector<double> lr(nl), ls(nl), lt(nl);
+      // the 1-D problems depend only on the boundary flags and the three
+      // lengths: each distinct one is solved once (bit-identical reuse)
+      typedef std::tuple<int, int, uint64_t, uint64_t, uint64_t> Key;
+      std::map<Key, std::pair<std::vector<double>, std::vector<double>>> memo;
+      auto bits = [](double v) {
+        uint64_t u;
+        std::memcpy(&u, &v, sizeof(u));
+        return u;
+      };
+      auto fast1d_once = [&](double *s1, double *lam, int lbc, int rbc, double ll,
+                             double lrr_) -> int {
+        const Key key(lbc, rbc, bits(ll), bits(lm), bits(lrr_));
+        auto it = memo.find(key);
+        if (it == memo.end()) {
+          std::vector<double> sv(size_t(2) * nl * nl), lv(nl);
+          NB_TRY(fast1d(sv.data(), lv.data(), nl, lbc, rbc, ll, lm, lrr_, ah[l].data(),
+                        bh[l].data(), n));
+          it = memo.emplace(key, std::make_pair(std::move(sv), std::move(lv))).first;
+        }
+        std::copy(it->second.first.begin(), it->second.first.end(), s1);
+        std::copy(it->second.second.begin(), it->second.second.end(), lam);
+        return NB_OK;
+      };
       for (int e = 0; e < nelt; ++e) {
         const double llr = at(1, 2, 2, e) - lm, lrr = at(lx, 2, 2, e) - lm;
         const double lls = at(2, 1, 2, e) - lm, lrs = at(2, lx, 2, e) - lm;
         const double llt = at(2, 2, 1, e) - lm, lrt = at(2, 2, lx, e) - lm;
         const unsigned f = op.face[e];
         double *se = S.data() + size_t(nl) * nl * 6 * e;
-        NB_TRY(fast1d(se, lr.data(), nl, f & 1u ? 1 : 0, f & 2u ? 1 : 0, llr, lm, lrr,
-                      ah[l].data(), bh[l].data(), n));
-        NB_TRY(fast1d(se + 2 * nl * nl, ls.data(), nl, f & 4u ? 1 : 0, f & 8u ? 1 : 0, lls,
-                      lm, lrs, ah[l].data(), bh[l].data(), n));
-        NB_TRY(fast1d(se + 4 * nl * nl, lt.data(), nl, f & 16u ? 1 : 0, f & 32u ? 1 : 0, llt,
-                      lm, lrt, ah[l].data(), bh[l].data(), n));
+        NB_TRY(fast1d_once(se, lr.data(), f & 1u ? 1 : 0, f & 2u ? 1 : 0, llr, lrr));
+        NB_TRY(fast1d_once(se + 2 * nl * nl, ls.data(), f & 4u ? 1 : 0, f & 8u ? 1 : 0, lls,
+                           lrs));
+        NB_TRY(fast1d_once(se + 4 * nl * nl, lt.data(), f & 16u ? 1 : 0, f & 32u ? 1 : 0,
+                           llt, lrt));
         auto vmax = [&](const std::vector<double> &v) {
           double t = -99.0e20;
           for (int q = 1; q <= nl - 2; ++q) t = std::max(t, v[q]);

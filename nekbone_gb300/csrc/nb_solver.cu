@@ -308,8 +308,10 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
   set_vert_box(glo.data(), lx, int(nelt), nelx, nely, lglel.data());
   GsHost maps;
   gs_topology(glo.data(), int(n), &maps);
-  return operator_from(op, nelx, nely, nelz, int(nelt), lx, lglel.data(),
-                       d.data(), maps, mask_mode, s);
+  NB_TRY(operator_from(op, nelx, nely, nelz, int(nelt), lx, lglel.data(), d.data(), maps,
+                       mask_mode, s));
+  op->brick = true;
+  return NB_OK;
 }
 
 int ensure_host_maps(Operator &op) {

@@ -43,6 +43,7 @@ struct Operator {
   int *bnd_off = nullptr;
   unsigned *bnd_idx = nullptr;      // with mask flags in bit 31
   cudaStream_t stream = nullptr;
+  bool brick = false;               // box in the brick element order (lglel(e) = e)
 
   ~Operator();
 };
@@ -87,6 +88,9 @@ int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
 // device without a sort (nb_topo.cu).  The host jl maps stay empty until
 // ensure_host_maps builds them.
 int box_topology_device(Operator *op, cudaStream_t s);
+// The gather-scatter CSR alone for lx points per element direction on the
+// same brick (the multigrid levels' regular and extended numberings).
+int box_gs_device(int lx, int nelx, int nely, int nelz, GsDevice *g, cudaStream_t s);
 int ensure_host_maps(Operator &op);
 // Whether operator_box builds full-mask topologies on the device (default
 // on); the host path (jl's sort-based construction) stays available.

@@ -188,14 +188,14 @@ __global__ void __launch_bounds__(kThr)
       pos[0] += 1;
       pos[1] += pi.m;
     }
-    if (pi.primary && pi.boundary) {
+    if (bd_off && pi.primary && pi.boundary) {
       bd_off[pos[2]] = pos[3];
       for (int k = 0; k < pi.m; ++k)
         bd_idx[pos[3] + k] = unsigned(pi.q[k]) | (pi.masked ? 0x80000000u : 0u);
       pos[2] += 1;
       pos[3] += pi.m;
     }
-    if (pi.masked) mask[pos[4]++] = int(q);
+    if (mask && pi.masked) mask[pos[4]++] = int(q);
   }
 }
 
@@ -206,11 +206,14 @@ bool g_setup_on_device = true;
 bool setup_on_device() { return g_setup_on_device; }
 void set_setup_on_device(bool on) { g_setup_on_device = on; }
 
-int box_topology_device(Operator *op, cudaStream_t s) {
-  const Box b{op->lx, op->nelx, op->nely, op->nelz, op->n};
-  if (op->n >= (1L << 31))
-    return fail(NB_ERR_UNSUPPORTED, "device topology: n = %ld exceeds 2^31-1", op->n);
-  const int nb = int((op->n + kBlk - 1) / kBlk);
+namespace {
+
+// The sweep for lx points per element direction; bnd/mask outputs are
+// produced only when op is given.
+int topology_sweep(const Box &b, GsDevice *g, Operator *op, cudaStream_t s) {
+  if (b.n >= (1L << 31))
+    return fail(NB_ERR_UNSUPPORTED, "device topology: n = %ld exceeds 2^31-1", b.n);
+  const int nb = int((b.n + kBlk - 1) / kBlk);
   int *blocksum = nullptr;
   long *total = nullptr;
   NB_CUDA(cudaMalloc(&blocksum, size_t(5) * nb * sizeof(int)));
@@ -227,32 +230,48 @@ int box_topology_device(Operator *op, cudaStream_t s) {
     cudaFree(total);
     return fail(NB_ERR_CUDA, "device topology: %s", cudaGetErrorString(e));
   }
-  GsDevice &g = op->gs;
-  g = GsDevice();
-  g.n = int(op->n);
-  g.symmetric = true;
-  g.ng = int(tot[0]);
-  op->nbg = int(tot[2]);
-  op->n_mask = int(tot[4]);
-  NB_CUDA(cudaMalloc(&g.off, (tot[0] + 1) * sizeof(int)));
-  NB_CUDA(cudaMalloc(&g.idx, std::max(1L, tot[1]) * sizeof(int)));
-  NB_CUDA(cudaMalloc(&op->bnd_off, (tot[2] + 1) * sizeof(int)));
-  NB_CUDA(cudaMalloc(&op->bnd_idx, std::max(1L, tot[3]) * sizeof(unsigned)));
-  NB_CUDA(cudaMalloc(&op->d_mask_list, std::max(1L, tot[4]) * sizeof(int)));
-  k_topo_emit<<<nb, kThr, 0, s>>>(b, blocksum, g.off, g.idx, op->bnd_off, op->bnd_idx,
-                                  op->d_mask_list);
+  *g = GsDevice();
+  g->n = int(b.n);
+  g->symmetric = true;
+  g->ng = int(tot[0]);
+  NB_CUDA(cudaMalloc(&g->off, (tot[0] + 1) * sizeof(int)));
+  NB_CUDA(cudaMalloc(&g->idx, std::max(1L, tot[1]) * sizeof(int)));
+  if (op) {
+    op->nbg = int(tot[2]);
+    op->n_mask = int(tot[4]);
+    NB_CUDA(cudaMalloc(&op->bnd_off, (tot[2] + 1) * sizeof(int)));
+    NB_CUDA(cudaMalloc(&op->bnd_idx, std::max(1L, tot[3]) * sizeof(unsigned)));
+    NB_CUDA(cudaMalloc(&op->d_mask_list, std::max(1L, tot[4]) * sizeof(int)));
+  }
+  k_topo_emit<<<nb, kThr, 0, s>>>(b, blocksum, g->off, g->idx, op ? op->bnd_off : nullptr,
+                                  op ? op->bnd_idx : nullptr, op ? op->d_mask_list : nullptr);
   const int end_gs = int(tot[1]), end_bd = int(tot[3]);
-  NB_CUDA(cudaMemcpyAsync(g.off + tot[0], &end_gs, sizeof(int), cudaMemcpyHostToDevice, s));
-  NB_CUDA(cudaMemcpyAsync(op->bnd_off + tot[2], &end_bd, sizeof(int), cudaMemcpyHostToDevice,
-                          s));
+  NB_CUDA(cudaMemcpyAsync(g->off + tot[0], &end_gs, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (op)
+    NB_CUDA(cudaMemcpyAsync(op->bnd_off + tot[2], &end_bd, sizeof(int),
+                            cudaMemcpyHostToDevice, s));
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   cudaFree(blocksum);
   cudaFree(total);
   if (e != cudaSuccess) return fail(NB_ERR_CUDA, "device topology: %s", cudaGetErrorString(e));
+  return NB_OK;
+}
+
+}  // namespace
+
+int box_topology_device(Operator *op, cudaStream_t s) {
+  const Box b{op->lx, op->nelx, op->nely, op->nelz, op->n};
+  NB_TRY(topology_sweep(b, &op->gs, op, s));
   op->fused_ok = true;
   op->mask_built = true;
+  op->brick = true;
   return NB_OK;
+}
+
+int box_gs_device(int lx, int nelx, int nely, int nelz, GsDevice *g, cudaStream_t s) {
+  const Box b{lx, nelx, nely, nelz, long(nelx) * nely * nelz * lx * lx * lx};
+  return topology_sweep(b, g, nullptr, s);
 }
 
 }  // namespace nb
