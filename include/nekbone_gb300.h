@@ -248,6 +248,14 @@ int nb_glsc3_noalloc(const double *a, const double *b, const double *mult,
  * in FP64. */
 int nb_mg_setup(nb_mesh *mesh, const int *orders, int nlev, int precision);
 /* z = M^-1 rhs (h1mg_solve, hsmg.f:960-1034); masks rhs in place */
+/* Replaces the coarse "solve" of the V-cycle (a copy plus dssum in the
+ * reference, hsmg.f:945-957) by an exact FP64 solve of the Galerkin coarse
+ * operator R A P on the unmasked vertices, for the metric g: the V-cycle's
+ * own restriction and interpolation chain around the FP64 operator, probed
+ * with 27 colourings of the vertex grid, checked and densely inverted.  Box
+ * meshes, mask_mode 1, the coarsest level of order 1, at most 16384 coarse
+ * unknowns.  No counterpart in the reference. */
+int nb_mg_setup_coarse(nb_mesh *mesh, const double *g);
 int nb_mg_solve(nb_mesh *mesh, double *z, double *rhs);
 /* FP64 CG preconditioned with the mesh's hsmg until
  * sqrt(r'Cr)/sqrt(r0'Cr0) <= tol (max_iter cap; residual polled every

@@ -55,6 +55,7 @@ EXPORTS = (
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
+    "nb_mg_setup_coarse",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -122,6 +123,8 @@ lib.nb_set_setup_on_device.argtypes = [_i]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
+lib.nb_mg_setup_coarse.restype = _i
+lib.nb_mg_setup_coarse.argtypes = [_p, _p]
 lib.nb_mesh_mask_list.restype = _i
 lib.nb_mesh_mask_list.argtypes = [_p, _p, _p]
 #: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
@@ -493,6 +496,10 @@ class DeviceMesh:
         else:
             o = _np.ascontiguousarray(orders, dtype=_np.int32)
             _check(lib.nb_mg_setup(self._h, _ptr(o), len(o), precision))
+
+    def mg_setup_coarse(self, g) -> None:
+        """Exact Galerkin coarse solve for metric g (after mg_setup)."""
+        _check(lib.nb_mg_setup_coarse(self._h, _p(g)))
 
     def mg_solve(self, z, rhs) -> None:
         _check(lib.nb_mg_solve(self._h, _p(z), _p(rhs)))

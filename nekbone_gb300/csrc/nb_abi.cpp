@@ -952,6 +952,13 @@ int nb_mg_setup(nb_mesh *mesh, const int *orders, int nlev, int precision) {
   return NB_OK;
 }
 
+int nb_mg_setup_coarse(nb_mesh *mesh, const double *g) {
+  clear_status();
+  if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  if (!mesh->mg) return fail(NB_ERR_STATE, "nb_mg_setup_coarse: call nb_mg_setup first");
+  return mg_setup_coarse(mesh->mg.get(), g, st().s);
+}
+
 int nb_mg_solve(nb_mesh *mesh, double *z, double *rhs) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
@@ -970,11 +977,9 @@ int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
   CgWork &wk = mesh->wk;
   const long n = op.n;
   if (check_every < 1) check_every = 1;
-  double *r = nullptr, *w = nullptr, *p = nullptr, *z = nullptr;
-  NB_CUDA(cudaMalloc(&r, n * 8));
-  NB_CUDA(cudaMalloc(&w, n * 8));
-  NB_CUDA(cudaMalloc(&p, n * 8));
-  NB_CUDA(cudaMalloc(&z, n * 8));
+  NB_TRY(wk.ensure_scratch(size_t(4) * n * 8));
+  double *r = reinterpret_cast<double *>(wk.scratch);
+  double *w = r + n, *p = w + n, *z = p + n;
   MgPrecond M(mesh->mg.get());
   int done = 0, stt = NB_OK;
   double rn0 = 0.0, rn = 0.0;
@@ -991,10 +996,6 @@ int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
       stt = fail(NB_ERR_CUDA, "nb_pcg_tol: reading rnorm");
     if (rn0 > 0 && rn / rn0 <= tol) break;
   }
-  cudaFree(r);
-  cudaFree(w);
-  cudaFree(p);
-  cudaFree(z);
   if (stt) return stt;
   if (iters) *iters = done;
   if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;

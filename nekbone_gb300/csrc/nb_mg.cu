@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <tuple>
 
 #include "nb_mg.h"
@@ -41,6 +42,11 @@ Multigrid::~Multigrid() {
   if (A_f) cudaFree(A_f);
   if (B_f) cudaFree(B_f);
   if (z_f) cudaFree(z_f);
+  if (c_ainv) cudaFree(c_ainv);
+  if (c_gid) cudaFree(c_gid);
+  if (c_prim) cudaFree(c_prim);
+  if (c_b) cudaFree(c_b);
+  if (c_x) cudaFree(c_x);
 }
 
 namespace {
@@ -813,6 +819,44 @@ __global__ void k_to_f64(double *y, const float *x, long n) {
     y[q] = double(x[q]);
 }
 
+// ---- exact coarse solve ----------------------------------------------------
+// b(i) = assembled residual at coarse vertex i (its first copy after dssum)
+__global__ void k_coarse_gather(double *b, const double *e1, const int *prim, int nc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nc) b[i] = e1[prim[i]];
+}
+// e1(q) = x(gid(q)), 0 at masked points
+__global__ void k_coarse_scatter(double *e1, const double *x, const int *gid, long n1) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n1;
+       q += long(gridDim.x) * blockDim.x) {
+    const int c = gid[q];
+    e1[q] = c >= 0 ? x[c] : 0.0;
+  }
+}
+// y = A x for the dense inverse: one warp per row, lane-strided partial
+// sums in a fixed order, then a fixed shuffle tree
+__global__ void __launch_bounds__(256) k_dense_mv(double *y, const double *A,
+                                                  const double *x, int n) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double *row = A + size_t(warp) * n;
+  double acc = 0.0;
+  for (int j = lane; j < n; j += 32) acc = fma_rn(row[j], x[j], acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) y[warp] = acc;
+}
+
+int coarse_apply(Multigrid &mg, cudaStream_t s) {
+  MgLevel &C = mg.lv[1];
+  k_coarse_gather<<<(mg.nc + 255) / 256, 256, 0, s>>>(mg.c_b, C.e, mg.c_prim, mg.nc);
+  k_dense_mv<<<(mg.nc * 32 + 255) / 256, 256, 0, s>>>(mg.c_x, mg.c_ainv, mg.c_b, mg.nc);
+  k_coarse_scatter<<<grid_for(C.n), 256, 0, s>>>(C.e, mg.c_x, mg.c_gid, C.n);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
 // The V-cycle of h1mg_solve (hsmg.f:960-1034) in precision T from level Lm
 // down; the coarse "solve" (copy + dssum + mask, hsmg.f:945-957) is always
 // FP64.  rT is the top-level right-hand side (already masked), zT the result.
@@ -834,6 +878,7 @@ int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
     NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
     NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));  // hsmg_coarse_solve
     NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
+    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s));
     NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
   } else {
     // FP64 coarse solve between the FP32 legs
@@ -841,6 +886,7 @@ int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
     NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
     NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));
     NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
+    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s));
     NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
     k_to_f32<<<grid_for(C.n), 256, 0, s>>>(C.e_f, C.e, C.n);
     NB_CUDA(cudaGetLastError());
@@ -851,6 +897,206 @@ int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
 }
 
 }  // namespace
+
+// R A P of the V-cycle's transfers on a level-1 vector x1 (local copies):
+// the result r1 is assembled (dssum) and masked, as the coarse step sees it.
+static int coarse_rap(Multigrid &mg, const double *g, double *x1, double *z, double *w,
+                      cudaStream_t s) {
+  const Operator &op = *mg.op;
+  const int L = mg.nlev;
+  // P: e_2 = J e_1, ..., z = J e_{L-1} (the unwinding of h1mg_solve)
+  const double *src = x1;
+  for (int l = 2; l < L; ++l) {
+    NB_CUDA(cudaMemsetAsync(mg.lv[l].e, 0, mg.lv[l].n * sizeof(double), s));
+    NB_TRY(mg_intp_add<double>(mg, mg.lv[l].e, src, l - 1, s));
+    src = mg.lv[l].e;
+  }
+  NB_CUDA(cudaMemsetAsync(z, 0, op.n * sizeof(double), s));
+  NB_TRY(mg_intp_add<double>(mg, z, src, L - 1, s));
+  // A
+  NB_TRY(apply_ax<double>(op, w, z, g, s));
+  // R: the downward leg, masked at every level as h1mg_schwarz masks r
+  MgLevel &Top = mg.lv[L];
+  NB_TRY(vec_mask<double>(w, Top.mask, Top.nmask, s));
+  NB_TRY(vec_copy<double>(Top.r, w, Top.n, s));
+  for (int l = L - 1; l >= 2; --l) {
+    NB_TRY(mg_rstr<double>(mg, mg.lv[l].r, mg.lv[l + 1].r, l, true, s));
+    NB_TRY(vec_mask<double>(mg.lv[l].r, mg.lv[l].mask, mg.lv[l].nmask, s));
+  }
+  MgLevel &C = mg.lv[1];
+  NB_TRY(mg_rstr<double>(mg, C.r, mg.lv[2].r, 1, false, s));
+  NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
+  NB_TRY(gs_exec(C.gs, C.r, 1, 1, 0, s));
+  return NB_OK;
+}
+
+int mg_setup_coarse(Multigrid *mg, const double *g, cudaStream_t s) {
+  const Operator &op = *mg->op;
+  MgLevel &C = mg->lv[1];
+  if (C.nh != 2)
+    return fail(NB_ERR_UNSUPPORTED, "exact coarse solve: the coarsest level must be order 1");
+  if (!op.brick || op.mask_mode != 1)
+    return fail(NB_ERR_UNSUPPORTED, "exact coarse solve: box meshes with the full mask only");
+  const int nx = op.nelx, ny = op.nely, nz = op.nelz, nelt = op.nelt;
+  const int vx = nx + 1, vy = ny + 1, vz = nz + 1;
+  const long nv = long(vx) * vy * vz;
+  // unmasked vertices, compressed in lexicographic order
+  std::vector<int> cidx(nv, -1);
+  std::vector<int> cv;  // coarse index -> vertex
+  for (int k = 1; k < vz - 1; ++k)
+    for (int j = 1; j < vy - 1; ++j)
+      for (int i = 1; i < vx - 1; ++i) {
+        const long v = i + long(vx) * (j + long(vy) * k);
+        cidx[v] = int(cv.size());
+        cv.push_back(int(v));
+      }
+  const int nc = int(cv.size());
+  if (nc == 0) return fail(NB_ERR_UNSUPPORTED, "exact coarse solve: no interior vertex");
+  if (nc > kMaxCoarse)
+    return fail(NB_ERR_UNSUPPORTED, "exact coarse solve: %d coarse unknowns (at most %d)", nc,
+                kMaxCoarse);
+  const long n1 = C.n;  // 8 * nelt
+  std::vector<int> gid(n1, -1), prim(nc, -1);
+  std::vector<int> vert(n1);
+  for (int e = 0; e < nelt; ++e) {
+    const int ex = e % nx, ey = (e / nx) % ny, ez = e / (nx * ny);
+    for (int q = 0; q < 8; ++q) {
+      const int i = q & 1, j = (q >> 1) & 1, k = q >> 2;
+      const long v = (ex + i) + long(vx) * ((ey + j) + long(vy) * (ez + k));
+      const long lq = long(8) * e + q;
+      vert[lq] = int(v);
+      gid[lq] = cidx[v];
+      if (cidx[v] >= 0 && prim[cidx[v]] < 0) prim[cidx[v]] = int(lq);
+    }
+  }
+  double *x1 = nullptr, *z = nullptr, *w = nullptr;
+  NB_CUDA(cudaMalloc(&x1, n1 * sizeof(double)));
+  NB_CUDA(cudaMalloc(&z, op.n * sizeof(double)));
+  NB_CUDA(cudaMalloc(&w, op.n * sizeof(double)));
+  int st = NB_OK;
+  // probes: 27 colourings, (vx mod 3, vy mod 3, vz mod 3)
+  std::vector<double> A(size_t(nc) * nc, 0.0), hx(n1), hr(n1);
+  for (int c = 0; c < 27 && !st; ++c) {
+    const int cx = c % 3, cy = (c / 3) % 3, cz = c / 9;
+    for (long q = 0; q < n1; ++q) {
+      const int v = vert[q];
+      const int ix = v % vx, iy = (v / vx) % vy, iz = v / (vx * vy);
+      hx[q] = (gid[q] >= 0 && ix % 3 == cx && iy % 3 == cy && iz % 3 == cz) ? 1.0 : 0.0;
+    }
+    if (cudaMemcpy(x1, hx.data(), n1 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      st = fail(NB_ERR_CUDA, "exact coarse solve: upload");
+    if (!st) st = coarse_rap(*mg, g, x1, z, w, s);
+    if (!st && (cudaMemcpyAsync(hr.data(), C.r, n1 * sizeof(double), cudaMemcpyDeviceToHost,
+                                s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess))
+      st = fail(NB_ERR_CUDA, "exact coarse solve: probe");
+    for (int i = 0; i < nc && !st; ++i) {
+      const int v = cv[i];
+      const int ix = v % vx, iy = (v / vx) % vy, iz = v / (vx * vy);
+      // the one vertex of this colour within distance 1
+      auto pick = [](int a, int col) {
+        for (int d = -1; d <= 1; ++d)
+          if (((a + d) % 3 + 3) % 3 == col) return a + d;
+        return -1;
+      };
+      const int jx = pick(ix, cx), jy = pick(iy, cy), jz = pick(iz, cz);
+      if (jx < 0 || jy < 0 || jz < 0 || jx >= vx || jy >= vy || jz >= vz) continue;
+      const int cj = cidx[jx + long(vx) * (jy + long(vy) * jz)];
+      if (cj < 0) continue;
+      A[size_t(i) * nc + cj] = hr[prim[i]];
+    }
+  }
+  // check: the probed matrix reproduces R A P on a random vector
+  if (!st) {
+    uint64_t z64 = 0x9E3779B97F4A7C15ull;
+    std::vector<double> xc(nc);
+    for (int i = 0; i < nc; ++i) {
+      z64 ^= z64 << 13, z64 ^= z64 >> 7, z64 ^= z64 << 17;
+      xc[i] = double(z64 >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    }
+    for (long q = 0; q < n1; ++q) hx[q] = gid[q] >= 0 ? xc[gid[q]] : 0.0;
+    if (cudaMemcpy(x1, hx.data(), n1 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+      st = fail(NB_ERR_CUDA, "exact coarse solve: upload");
+    if (!st) st = coarse_rap(*mg, g, x1, z, w, s);
+    if (!st && (cudaMemcpyAsync(hr.data(), C.r, n1 * sizeof(double), cudaMemcpyDeviceToHost,
+                                s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess))
+      st = fail(NB_ERR_CUDA, "exact coarse solve: check");
+    double emax = 0.0, ymax = 0.0, amax = 0.0, asym = 0.0;
+    for (int i = 0; i < nc && !st; ++i) {
+      double y = 0.0;
+      for (int j = 0; j < nc; ++j) y += A[size_t(i) * nc + j] * xc[j];
+      emax = std::max(emax, std::fabs(y - hr[prim[i]]));
+      ymax = std::max(ymax, std::fabs(hr[prim[i]]));
+    }
+    for (int i = 0; i < nc && !st; ++i)
+      for (int j = 0; j < i; ++j) {
+        amax = std::max(amax, std::fabs(A[size_t(i) * nc + j]));
+        asym = std::max(asym, std::fabs(A[size_t(i) * nc + j] - A[size_t(j) * nc + i]));
+      }
+    if (!st && emax > 1e-10 * ymax)
+      st = fail(NB_ERR_NUMERIC, "exact coarse solve: probing mismatch %.3e", emax / ymax);
+    if (!st && asym > 1e-10 * amax)
+      st = fail(NB_ERR_NUMERIC, "exact coarse solve: R A P not symmetric (%.3e)", asym / amax);
+  }
+  cudaFree(x1);
+  cudaFree(z);
+  cudaFree(w);
+  if (st) return st;
+  // symmetrise, banded Cholesky, dense inverse (columns in parallel)
+  int bw = 0;
+  for (int i = 0; i < nc; ++i)
+    for (int j = 0; j < i; ++j) {
+      const double a = 0.5 * (A[size_t(i) * nc + j] + A[size_t(j) * nc + i]);
+      A[size_t(i) * nc + j] = A[size_t(j) * nc + i] = a;
+      if (a != 0.0) bw = std::max(bw, i - j);
+    }
+  std::vector<double> Lb(size_t(nc) * (bw + 1), 0.0);  // L(i, i-k) at [i*(bw+1)+k]
+  auto Lat = [&](int i, int j) -> double & { return Lb[size_t(i) * (bw + 1) + (i - j)]; };
+  for (int i = 0; i < nc; ++i)
+    for (int j = std::max(0, i - bw); j <= i; ++j) {
+      double sum = A[size_t(i) * nc + j];
+      for (int k = std::max(std::max(0, i - bw), j - bw); k < j; ++k) sum -= Lat(i, k) * Lat(j, k);
+      if (i == j) {
+        if (!(sum > 0.0)) return fail(NB_ERR_NUMERIC, "exact coarse solve: not positive definite");
+        Lat(i, i) = std::sqrt(sum);
+      } else {
+        Lat(i, j) = sum / Lat(j, j);
+      }
+    }
+  std::vector<double> inv(size_t(nc) * nc);
+  const int nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  std::vector<std::thread> th;
+  for (int t = 0; t < nth; ++t)
+    th.emplace_back([&, t]() {
+      std::vector<double> y(nc);
+      for (int col = t; col < nc; col += nth) {
+        // L y = e_col
+        for (int i = 0; i < nc; ++i) {
+          double sum = i == col ? 1.0 : 0.0;
+          for (int k = std::max(0, i - bw); k < i; ++k) sum -= Lat(i, k) * y[k];
+          y[i] = sum / Lat(i, i);
+        }
+        // L^T x = y
+        for (int i = nc - 1; i >= 0; --i) {
+          double sum = y[i];
+          for (int k = i + 1; k <= std::min(nc - 1, i + bw); ++k) sum -= Lat(k, i) * y[k];
+          y[i] = sum / Lat(i, i);
+        }
+        for (int i = 0; i < nc; ++i) inv[size_t(i) * nc + col] = y[i];
+      }
+    });
+  for (auto &t : th) t.join();
+  NB_TRY(upload(&mg->c_ainv, inv));
+  NB_TRY(upload(&mg->c_gid, gid));
+  NB_TRY(upload(&mg->c_prim, prim));
+  NB_TRY(dmalloc(&mg->c_b, nc));
+  NB_TRY(dmalloc(&mg->c_x, nc));
+  mg->nc = nc;
+  mg->coarse_exact = true;
+  NB_CUDA(cudaStreamSynchronize(s));
+  return NB_OK;
+}
 
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s) {
   if (mg.precision == 64) return vcycle<double>(mg, z, rhs, s);

@@ -34,6 +34,15 @@ struct Multigrid {
   double *w = nullptr;            // interpolation result
   int precision = 64;             // 64, or 32: FP32 Schwarz smoother and transfers
   float *A_f = nullptr, *B_f = nullptr, *z_f = nullptr;
+  // exact coarse solve (replacing the reference's copy + dssum): the
+  // Galerkin operator R A P of the V-cycle's own transfer chain on the
+  // unmasked vertices, probed with 27 colours, inverted densely
+  bool coarse_exact = false;
+  int nc = 0;                     // unmasked coarse vertices
+  double *c_ainv = nullptr;       // nc x nc inverse, row-major (symmetric)
+  int *c_gid = nullptr;           // level-1 local point -> coarse index or -1
+  int *c_prim = nullptr;          // coarse index -> its first level-1 copy
+  double *c_b = nullptr, *c_x = nullptr;
   ~Multigrid();
 };
 
@@ -42,6 +51,14 @@ struct Multigrid {
 // otherwise nlev polynomial orders, coarsest first, the last = lx1-1.
 int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
              cudaStream_t s, int precision = 64);
+// Replaces the coarse "solve" (hsmg.f:945-957) by an exact solve of the
+// Galerkin coarse operator for the metric g (FP64): probes R A P with 27
+// colourings of the vertex grid, checks it reproduces R A P on a random
+// vector and is symmetric, factors it (banded Cholesky) and keeps the dense
+// inverse.  Box meshes in brick order, mask_mode 1, at most
+// kMaxCoarse unknowns.
+constexpr int kMaxCoarse = 16384;
+int mg_setup_coarse(Multigrid *mg, const double *g, cudaStream_t s);
 // h1mg_solve (hsmg.f:960-1034): z = M^-1 rhs; masks rhs in place.
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s);
 
