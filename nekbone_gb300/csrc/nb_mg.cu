@@ -106,44 +106,42 @@ __device__ inline int ghost_face(int a, int b, int c, int nl) {
 // element's own layer-2 value, ghost edges and corners zero.
 template <typename T>
 __global__ void k_toext(T *A, const T *r, int nh, int nelt) {
+  // 32-bit indices (extended vectors stay below 2^31 points): the 64-bit
+  // division per point made this pass integer-bound
   const int nl = nh + 2;
-  const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh;
-  const long tot = nl3 * nelt;
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
-       q += long(gridDim.x) * blockDim.x) {
-    const long e = q / nl3;
-    const int rr = int(q % nl3);
+  const int nl3 = nl * nl * nl, nh3 = nh * nh * nh;
+  const int tot = nl3 * nelt;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
+    const int e = q / nl3;
+    const int rr = q - e * nl3;
     int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
     const int gf = ghost_face(a, b, c, nl);
     T v = T(0);
     if (a >= 1 && a <= nh && b >= 1 && b <= nh && c >= 1 && c <= nh) {
-      v = r[e * nh3 + (a - 1) + nh * (b - 1) + long(nh) * nh * (c - 1)];
+      v = r[e * nh3 + (a - 1) + nh * (b - 1) + nh * nh * (c - 1)];
     } else if (gf) {
       if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
       else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
       else if (gf == 5) c = 2; else c = nl - 3;
-      v = r[e * nh3 + (a - 1) + nh * (b - 1) + long(nh) * nh * (c - 1)];
+      v = r[e * nh3 + (a - 1) + nh * (b - 1) + nh * nh * (c - 1)];
     }
     A[q] = v;
   }
 }
 
-// extrude(A,0,1,A,2,-1) (hsmg.f:1079): ghost faces minus the own layer-2
-// value, leaving the neighbour's value
 template <typename T>
 __global__ void k_ghost_minus(T *A, int nh, int nelt) {
   const int nl = nh + 2;
-  const long nl3 = long(nl) * nl * nl, tot = nl3 * nelt;
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
-       q += long(gridDim.x) * blockDim.x) {
-    const int rr = int(q % nl3);
+  const int nl3 = nl * nl * nl, tot = nl3 * nelt;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
+    const int rr = q % nl3;
     int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
     const int gf = ghost_face(a, b, c, nl);
     if (!gf) continue;
     if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
     else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
     else if (gf == 5) c = 2; else c = nl - 3;
-    const long p = q - rr + a + long(nl) * b + long(nl) * nl * c;
+    const int p = q - rr + a + nl * b + nl * nl * c;
     A[q] = fma_rn(T(-1), A[p], A[q]);
   }
 }
@@ -183,21 +181,20 @@ __global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
 template <typename T>
 __global__ void k_overlap_toreg(T *e_out, const T *B, const T *A, int nh, int nelt) {
   const int nl = nh + 2;
-  const long nl3 = long(nl) * nl * nl, nh3 = long(nh) * nh * nh, tot = nh3 * nelt;
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
-       q += long(gridDim.x) * blockDim.x) {
-    const long e = q / nh3;
-    const int rr = int(q % nh3);
+  const int nl3 = nl * nl * nl, nh3 = nh * nh * nh, tot = nh3 * nelt;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
+    const int e = q / nh3;
+    const int rr = q - e * nh3;
     const int a = rr % nh + 1, b = (rr / nh) % nh + 1, c = rr / (nh * nh) + 1;
-    const long base = e * nl3;
-    auto at = [&](int x, int y, int z) { return base + x + long(nl) * y + long(nl) * nl * z; };
+    const int base = e * nl3;
+    auto at = [&](int x, int y, int z) { return base + x + nl * y + nl * nl * z; };
     T v = B[at(a, b, c)];
-    if (a == 2) { const long g = at(0, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (a == nl - 3) { const long g = at(nl - 1, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (b == 2) { const long g = at(a, 0, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (b == nl - 3) { const long g = at(a, nl - 1, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (c == 2) { const long g = at(a, b, 0); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (c == nl - 3) { const long g = at(a, b, nl - 1); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (a == 2) { const int g = at(0, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (a == nl - 3) { const int g = at(nl - 1, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (b == 2) { const int g = at(a, 0, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (b == nl - 3) { const int g = at(a, nl - 1, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (c == 2) { const int g = at(a, b, 0); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
+    if (c == nl - 3) { const int g = at(a, b, nl - 1); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
     e_out[q] = v;
   }
 }
@@ -205,13 +202,12 @@ __global__ void k_overlap_toreg(T *e_out, const T *B, const T *A, int nh, int ne
 // h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps
 template <typename T>
 __global__ void k_schwarz_wt(T *e, const T *wt, int n, int nelt) {
-  const long n3 = long(n) * n * n, tot = n3 * nelt;
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < tot;
-       q += long(gridDim.x) * blockDim.x) {
-    const long el = q / n3;
-    const int rr = int(q % n3);
+  const int n3 = n * n * n, tot = n3 * nelt;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
+    const int el = q / n3;
+    const int rr = q - el * n3;
     const int i = rr % n, j = (rr / n) % n, k = rr / (n * n);
-    const T *we = wt + el * 12L * n * n;
+    const T *we = wt + size_t(el) * 12 * n * n;
     auto W = [&](int a, int b, int s, int d) {
       return we[a + n * b + n * n * s + 4 * n * n * d];
     };
