@@ -101,53 +101,61 @@ __device__ inline int ghost_face(int a, int b, int c, int nl) {
   return 0;
 }
 
+// Grid for the line kernels below: one thread per (element, a, b) line of
+// n points, the c loop inside, so each thread splits its index once per
+// line rather than once per point (32-bit indices: MG vectors stay below
+// 2^31 points).  The c loop goes in chunks of kChunk points, all loads of a
+// chunk issued before its stores, so that each thread keeps several memory
+// requests in flight.
+constexpr int kChunk = 4;
+int grid_for(long n) { return int(std::max(1L, std::min<long>(152L * 8, (n + 255) / 256))); }
+inline int line_grid(int n, int nelt) { return grid_for(long(n) * n * nelt); }
+
 // h1mg_schwarz_toext3d + extrude(A,0,0,A,2,1) (hsmg.f:1075-1077): regular
 // points copied into the extended array, each ghost face set to the
 // element's own layer-2 value, ghost edges and corners zero.
 template <typename T>
 __global__ void k_toext(T *A, const T *r, int nh, int nelt) {
-  // 32-bit indices (extended vectors stay below 2^31 points): the 64-bit
-  // division per point made this pass integer-bound
-  const int nl = nh + 2;
-  const int nl3 = nl * nl * nl, nh3 = nh * nh * nh;
-  const int tot = nl3 * nelt;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
-    const int e = q / nl3;
-    const int rr = q - e * nl3;
-    int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
-    const int gf = ghost_face(a, b, c, nl);
-    T v = T(0);
-    if (a >= 1 && a <= nh && b >= 1 && b <= nh && c >= 1 && c <= nh) {
-      v = r[e * nh3 + (a - 1) + nh * (b - 1) + nh * nh * (c - 1)];
-    } else if (gf) {
-      if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
-      else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
-      else if (gf == 5) c = 2; else c = nl - 3;
-      v = r[e * nh3 + (a - 1) + nh * (b - 1) + nh * nh * (c - 1)];
+  const int nl = nh + 2, nl2 = nl * nl, nh2 = nh * nh, hi = nl - 1;
+  const int lines = nl2 * nelt;
+  // ghost coordinate 0 reads layer 2, nl-1 reads layer nl-3 (regular index - 1)
+  auto src = [&](int x) { return x == 0 ? 1 : (x == hi ? nh - 2 : x - 1); };
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
+    const int e = t / nl2, ab = t - e * nl2, a = ab % nl, b = ab / nl;
+    const int gab = (a == 0 || a == hi) + (b == 0 || b == hi);
+    const T *re = r + e * nh2 * nh + src(a) + nh * src(b);
+    T *Ae = A + e * nl2 * nl + ab;
+    for (int c0 = 0; c0 < nl; c0 += kChunk) {
+      T v[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) {
+        const int c = c0 + u;
+        const int g = gab + (c == 0 || c == hi);  // ghost coordinates of the point
+        v[u] = c < nl && g <= 1 ? re[nh2 * src(c)] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        if (c0 + u < nl) Ae[(c0 + u) * nl2] = v[u];
     }
-    A[q] = v;
   }
 }
 
+// extrude(A,0,1,A,2,-1) (hsmg.f:1079), applied by the FDM kernels as they
+// load A: a ghost-face value minus its layer-2 partner.
 template <typename T>
-__global__ void k_ghost_minus(T *A, int nh, int nelt) {
-  const int nl = nh + 2;
-  const int nl3 = nl * nl * nl, tot = nl3 * nelt;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
-    const int rr = q % nl3;
-    int a = rr % nl, b = (rr / nl) % nl, c = rr / (nl * nl);
-    const int gf = ghost_face(a, b, c, nl);
-    if (!gf) continue;
-    if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
-    else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
-    else if (gf == 5) c = 2; else c = nl - 3;
-    const int p = q - rr + a + nl * b + nl * nl * c;
-    A[q] = fma_rn(T(-1), A[p], A[q]);
-  }
+__device__ __forceinline__ T ghost_minus_at(const T *Ae, int a, int b, int c, int nl) {
+  const int gf = ghost_face(a, b, c, nl);
+  const T v = Ae[a + nl * b + nl * nl * c];
+  if (!gf) return v;
+  if (gf == 1) a = 2; else if (gf == 2) a = nl - 3;
+  else if (gf == 3) b = 2; else if (gf == 4) b = nl - 3;
+  else if (gf == 5) c = 2; else c = nl - 3;
+  return fma_rn(T(-1), Ae[a + nl * b + nl * nl * c], v);
 }
 
-// h1mg_do_fast (hsmg.f:1297-1318): B = S (d .* (S^T A)) per extended element;
-// also saves B's ghost faces into A (the first extrude of the overlap sum,
+// h1mg_do_fast (hsmg.f:1297-1318): B = S (d .* (S^T A')) per extended
+// element, A' being A with the ghost-face correction of hsmg.f:1079; also
+// saves B's ghost faces into A (the first extrude of the overlap sum,
 // hsmg.f:1084: A <- 0*A + B on the ghost faces).
 template <typename T>
 __global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
@@ -157,7 +165,8 @@ __global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
   T *u = sm, *v = u + nl3, *work = v + nl3, *work2 = work + nl3,
     *S = work2 + nl3;  // 6 matrices nl*nl
   const long e = blockIdx.x;
-  load_shared(u, A + e * nl3, nl3);
+  for (int q = threadIdx.x; q < nl3; q += blockDim.x)
+    u[q] = ghost_minus_at(A + e * nl3, q % nl, (q / nl) % nl, q / nl2, nl);
   load_shared(S, s + e * 6L * nl2, 6 * nl2);
   __syncthreads();
   // s(1,2,1)=S_r^T, s(1,1,2)=S_s, s(1,1,3)=S_t
@@ -174,56 +183,197 @@ __global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
   }
 }
 
+// The FDM tensor applies with the extended size NL known at compile time:
+// a work item is one 1-D line and a group of G of its outputs (independent
+// multiply-add chains), every loop fully unrolled with constant offsets.
+// Each output is the same left-to-right sum as tensor3's.  Two buffers
+// suffice: the input in X, the passes X -> Y -> X -> Y, the result in Y.
+template <typename T, int NL, int G>
+__device__ __forceinline__ void tensor3_fixed(T *X, T *Y, const T *A, const T *Bt,
+                                              const T *Ct) {
+  constexpr int NG = (NL + G - 1) / G;
+  const int t = threadIdx.x, nt = blockDim.x;
+  for (int it = t; it < NL * NL * NG; it += nt) {  // Y(a, np) = sum_m A(a,m) X(m, np)
+    const int np_ = it / NG, a0 = (it % NG) * G;
+    T x[NL];
+#pragma unroll
+    for (int m = 0; m < NL; ++m) x[m] = X[m + np_ * NL];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int a = a0 + g < NL ? a0 + g : NL - 1;
+      T acc = mul_rn(A[a], x[0]);
+#pragma unroll
+      for (int m = 1; m < NL; ++m) acc = fma_rn(A[a + m * NL], x[m], acc);
+      if (a0 + g < NL) Y[a + np_ * NL] = acc;
+    }
+  }
+  __syncthreads();
+  for (int it = t; it < NL * NL * NG; it += nt) {  // X(a,b,p) = sum_n Y(a,n,p) Bt(n,b)
+    const int ap = it / NG, b0 = (it % NG) * G;
+    const int a = ap % NL, p = ap / NL;
+    const T *wp = Y + NL * NL * p;
+    T x[NL];
+#pragma unroll
+    for (int n = 0; n < NL; ++n) x[n] = wp[a + n * NL];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int b = b0 + g < NL ? b0 + g : NL - 1;
+      T acc = mul_rn(x[0], Bt[b * NL]);
+#pragma unroll
+      for (int n = 1; n < NL; ++n) acc = fma_rn(x[n], Bt[n + b * NL], acc);
+      if (b0 + g < NL) X[a + NL * b + NL * NL * p] = acc;
+    }
+  }
+  __syncthreads();
+  for (int it = t; it < NL * NL * NG; it += nt) {  // Y(ab, c) = sum_p X(ab,p) Ct(p,c)
+    const int ab = it / NG, c0 = (it % NG) * G;
+    T x[NL];
+#pragma unroll
+    for (int p = 0; p < NL; ++p) x[p] = X[ab + p * NL * NL];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int c = c0 + g < NL ? c0 + g : NL - 1;
+      T acc = mul_rn(x[0], Ct[c * NL]);
+#pragma unroll
+      for (int p = 1; p < NL; ++p) acc = fma_rn(x[p], Ct[p + c * NL], acc);
+      if (c0 + g < NL) Y[ab + NL * NL * c] = acc;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int NL>
+__global__ void __launch_bounds__(256) k_fdm_fixed(T *B, T *A, const T *s, const T *d) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *sm = reinterpret_cast<T *>(sm_raw);
+  constexpr int NL2 = NL * NL, NL3 = NL2 * NL, G = NL >= 8 ? 4 : 2;
+  T *X = sm, *Y = X + NL3, *S = Y + NL3;
+  const int e = blockIdx.x;
+  for (int q = threadIdx.x; q < NL3; q += blockDim.x)
+    X[q] = ghost_minus_at(A + e * NL3, q % NL, (q / NL) % NL, q / NL2, NL);
+  load_shared(S, s + e * 6 * NL2, 6 * NL2);
+  __syncthreads();
+  tensor3_fixed<T, NL, G>(X, Y, S + NL2, S + 2 * NL2, S + 4 * NL2);
+  const T *de = d + e * NL3;
+  for (int q = threadIdx.x; q < NL3; q += blockDim.x) X[q] = mul_rn(de[q], Y[q]);
+  __syncthreads();
+  tensor3_fixed<T, NL, G>(X, Y, S, S + 3 * NL2, S + 5 * NL2);
+  for (int q = threadIdx.x; q < NL3; q += blockDim.x) {
+    const int a = q % NL, b = (q / NL) % NL, c = q / NL2;
+    B[e * NL3 + q] = Y[q];
+    if (ghost_face(a, b, c, NL)) A[e * NL3 + q] = Y[q];
+  }
+}
+
+// The fixed-size FDM kernel for an extended size nl (5..18), else null
+template <typename T>
+using FdmFn = void (*)(T *, T *, const T *, const T *);
+template <typename T>
+FdmFn<T> fdm_fixed(int nl) {
+  switch (nl) {
+#define NB_FDM(N) \
+  case N: return k_fdm_fixed<T, N>;
+    NB_FDM(5) NB_FDM(6) NB_FDM(7) NB_FDM(8) NB_FDM(9) NB_FDM(10) NB_FDM(11) NB_FDM(12)
+    NB_FDM(13) NB_FDM(14) NB_FDM(15) NB_FDM(16) NB_FDM(17) NB_FDM(18)
+#undef NB_FDM
+    default: return nullptr;
+  }
+}
+
+template <typename T>
+size_t fdm_smem(int nl) {
+  return sizeof(T) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
+}
+template <typename T>
+size_t fdm_fixed_smem(int nl) {
+  return sizeof(T) * (2 * size_t(nl) * nl * nl + 6 * nl * nl);
+}
+
+// FDM launch: the fixed-size kernel where one exists, else the general one
+// (shared-memory limits raised once in the set-up)
+template <typename T>
+int launch_fdm(T *B, T *A, const T *s, const T *d, int nl, int nelt, cudaStream_t st) {
+  if (FdmFn<T> fn = fdm_fixed<T>(nl)) fn<<<nelt, 256, fdm_fixed_smem<T>(nl), st>>>(B, A, s, d);
+  else k_fdm<T><<<nelt, 256, fdm_smem<T>(nl), st>>>(B, A, s, d, nl);
+  NB_CUDA(cudaGetLastError());
+  return NB_OK;
+}
+
 // extrude(B,0,1,A,0,-1), extrude(B,2,1,B,0,1), toreg3d (hsmg.f:1086-1090):
 // each regular point adds, in the reference's face order, the neighbour
 // contributions (gs'd ghost minus saved ghost) of the ghost faces whose
 // layer-2 partner it is.
 template <typename T>
 __global__ void k_overlap_toreg(T *e_out, const T *B, const T *A, int nh, int nelt) {
-  const int nl = nh + 2;
-  const int nl3 = nl * nl * nl, nh3 = nh * nh * nh, tot = nh3 * nelt;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
-    const int e = q / nh3;
-    const int rr = q - e * nh3;
-    const int a = rr % nh + 1, b = (rr / nh) % nh + 1, c = rr / (nh * nh) + 1;
-    const int base = e * nl3;
-    auto at = [&](int x, int y, int z) { return base + x + nl * y + nl * nl * z; };
-    T v = B[at(a, b, c)];
-    if (a == 2) { const int g = at(0, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (a == nl - 3) { const int g = at(nl - 1, b, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (b == 2) { const int g = at(a, 0, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (b == nl - 3) { const int g = at(a, nl - 1, c); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (c == 2) { const int g = at(a, b, 0); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    if (c == nl - 3) { const int g = at(a, b, nl - 1); v = add_rn(v, fma_rn(T(-1), A[g], B[g])); }
-    e_out[q] = v;
+  const int nl = nh + 2, nl2 = nl * nl, nh2 = nh * nh, lines = nh2 * nelt;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
+    const int e = t / nh2, ab = t - e * nh2, a = ab % nh + 1, b = ab / nh + 1;
+    const int base = e * nl2 * nl;
+    auto at = [&](int x, int y, int z) { return base + x + nl * y + nl2 * z; };
+    T *eo = e_out + e * nh2 * nh + ab;
+    for (int c0 = 1; c0 <= nh; c0 += kChunk) {
+      T v[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) {
+        const int c = c0 + u;
+        if (c > nh) break;
+        T x = B[at(a, b, c)];
+        if (a == 2) { const int g = at(0, b, c); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        if (a == nl - 3) { const int g = at(nl - 1, b, c); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        if (b == 2) { const int g = at(a, 0, c); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        if (b == nl - 3) { const int g = at(a, nl - 1, c); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        if (c == 2) { const int g = at(a, b, 0); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        if (c == nl - 3) { const int g = at(a, b, nl - 1); x = add_rn(x, fma_rn(T(-1), A[g], B[g])); }
+        v[u] = x;
+      }
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        if (c0 + u <= nh) eo[(c0 + u - 1) * nh2] = v[u];
+    }
   }
 }
 
-// h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps
+// h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps over
+// the layers L = {0, 1, n-2, n-1}: x faces, then y faces of the x-interior,
+// then z faces of the x- and y-interior.  A point takes the factors of
+// every layer slot s it sits in, in slot order (two slots coincide when
+// n < 4).  wt holds sqrt(wt), taken once at set-up in precision T.
 template <typename T>
 __global__ void k_schwarz_wt(T *e, const T *wt, int n, int nelt) {
-  const int n3 = n * n * n, tot = n3 * nelt;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += gridDim.x * blockDim.x) {
-    const int el = q / n3;
-    const int rr = q - el * n3;
-    const int i = rr % n, j = (rr / n) % n, k = rr / (n * n);
-    const T *we = wt + size_t(el) * 12 * n * n;
-    auto W = [&](int a, int b, int s, int d) {
-      return we[a + n * b + n * n * s + 4 * n * n * d];
-    };
-    const int L[4] = {0, 1, n - 2, n - 1};
-    T v = e[q];
-    bool done = false;
-    for (int s = 0; s < 4; ++s)
-      if (i == L[s]) { v = mul_rn(v, T(sqrt(W(j, k, s, 0)))); done = true; }
-    if (!done && i >= 2 && i <= n - 3) {
-      for (int s = 0; s < 4; ++s)
-        if (j == L[s]) { v = mul_rn(v, T(sqrt(W(i, k, s, 1)))); done = true; }
-      if (!done && j >= 2 && j <= n - 3)
-        for (int s = 0; s < 4; ++s)
-          if (k == L[s]) v = mul_rn(v, T(sqrt(W(i, j, s, 2))));
+  const int n2 = n * n, lines = n2 * nelt;
+  // bit s set: x sits in layer slot s
+  auto slots = [&](int x) {
+    return (x == 0) | (x == 1) << 1 | (x == n - 2) << 2 | (x == n - 1) << 3;
+  };
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
+    const int el = t / n2, ij = t - el * n2, i = ij % n, j = ij / n;
+    const int mi = slots(i), mj = slots(j);
+    // the sweep that owns the line's points (z: decided per point) and the
+    // face-array offset of its (a, b) pair
+    const int dir = mi ? 0 : mj ? 1 : 2;
+    const int m_line = mi ? mi : mj;
+    const T *we = wt + el * 12 * n2 + 4 * n2 * dir + (dir == 2 ? i + n * j : (dir == 1 ? i : j));
+    const int kstride = dir == 2 ? 0 : n;  // W(.,k,...) steps with k in sweeps 0 and 1
+    T *ee = e + el * n2 * n + ij;
+    for (int k0 = 0; k0 < n; k0 += kChunk) {
+      T v[kChunk];
+      int m[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u) {
+        const int k = k0 + u;
+        m[u] = k < n ? (dir == 2 ? slots(k) : m_line) : 0;
+        if (!m[u]) continue;
+        T x = ee[k * n2];
+        const T *wk = we + k * kstride;
+#pragma unroll
+        for (int sl = 0; sl < 4; ++sl)
+          if (m[u] >> sl & 1) x = mul_rn(x, wk[sl * n2]);
+        v[u] = x;
+      }
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        if (m[u]) ee[(k0 + u) * n2] = v[u];
     }
-    e[q] = v;
   }
 }
 
@@ -275,6 +425,144 @@ __global__ void k_intp_add(T *out, const T *uc, int nu, int nv, const T *jh, con
   tensor3<T>(vs, us, nv, nu, J, Jt, Jt, work, work2);
   for (int q = threadIdx.x; q < nv3; q += blockDim.x)
     out[e * nv3 + q] = add_rn(out[e * nv3 + q], vs[q]);
+}
+
+// Inter-level transfers with both sizes known at compile time: NU input
+// and NV output points per direction.  tensor3_fx makes the sums of tensor3
+// (same operands, same left-to-right order) with unrolled lines of G
+// outputs each; the last pass hands every output to store(q, value).
+template <typename T, int NV, int NU, int G, typename Store>
+__device__ __forceinline__ void tensor3_fx(const T *u, const T *A, const T *Bt, const T *Ct,
+                                           T *work, T *work2, Store store) {
+  constexpr int NG = (NV + G - 1) / G;
+  const int t = threadIdx.x, nt = blockDim.x;
+  for (int it = t; it < NU * NU * NG; it += nt) {  // work(a, np) = sum_m A(a,m) u(m, np)
+    const int np_ = it / NG, a0 = (it % NG) * G;
+    T x[NU];
+#pragma unroll
+    for (int m = 0; m < NU; ++m) x[m] = u[m + np_ * NU];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int a = a0 + g < NV ? a0 + g : NV - 1;
+      T acc = mul_rn(A[a], x[0]);
+#pragma unroll
+      for (int m = 1; m < NU; ++m) acc = fma_rn(A[a + m * NV], x[m], acc);
+      if (a0 + g < NV) work[a + np_ * NV] = acc;
+    }
+  }
+  __syncthreads();
+  for (int it = t; it < NV * NU * NG; it += nt) {  // work2(a,b,p) = sum_n work(a,n,p) Bt(n,b)
+    const int ap = it / NG, b0 = (it % NG) * G;
+    const int a = ap % NV, p = ap / NV;
+    const T *wp = work + NV * NU * p;
+    T x[NU];
+#pragma unroll
+    for (int n = 0; n < NU; ++n) x[n] = wp[a + n * NV];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int b = b0 + g < NV ? b0 + g : NV - 1;
+      T acc = mul_rn(x[0], Bt[b * NU]);
+#pragma unroll
+      for (int n = 1; n < NU; ++n) acc = fma_rn(x[n], Bt[n + b * NU], acc);
+      if (b0 + g < NV) work2[a + NV * b + NV * NV * p] = acc;
+    }
+  }
+  __syncthreads();
+  for (int it = t; it < NV * NV * NG; it += nt) {  // v(ab, c) = sum_p work2(ab,p) Ct(p,c)
+    const int ab = it / NG, c0 = (it % NG) * G;
+    T x[NU];
+#pragma unroll
+    for (int p = 0; p < NU; ++p) x[p] = work2[ab + p * NV * NV];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int c = c0 + g < NV ? c0 + g : NV - 1;
+      T acc = mul_rn(x[0], Ct[c * NU]);
+#pragma unroll
+      for (int p = 1; p < NU; ++p) acc = fma_rn(x[p], Ct[p + c * NU], acc);
+      if (c0 + g < NV) store(ab + NV * NV * c, acc);
+    }
+  }
+}
+
+template <int NV>
+constexpr int xfer_group() { return NV >= 8 ? 4 : 2; }
+
+template <typename T, int NU, int NV>
+constexpr size_t xfer_smem() {
+  return sizeof(T) * (NU * NU * NU + NV * NU * NU + NV * NV * NU + 2 * NU * NV);
+}
+
+// k_rstr with NU (fine) -> NV (coarse) fixed
+template <typename T, int NU, int NV>
+__global__ void __launch_bounds__(256) k_rstr_fixed(T *v, const T *u, const T *wt,
+                                                    const T *jht, const T *jh) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *us = reinterpret_cast<T *>(sm_raw), *work = us + NU * NU * NU, *work2 = work + NV * NU * NU,
+    *Jt = work2 + NV * NV * NU, *J = Jt + NU * NV;
+  constexpr int NU2 = NU * NU, NU3 = NU2 * NU, NV3 = NV * NV * NV;
+  const int e = blockIdx.x;
+  const T *we = wt + e * 6 * NU2;
+  for (int q = threadIdx.x; q < NU3; q += blockDim.x) {
+    const int i = q % NU, j = (q / NU) % NU, k = q / NU2;
+    T x = u[e * NU3 + q];
+    if (i == 0) x = mul_rn(x, we[j + NU * k + 0]);
+    else if (i == NU - 1) x = mul_rn(x, we[j + NU * k + NU2]);
+    else if (j == 0) x = mul_rn(x, we[i + NU * k + 2 * NU2]);
+    else if (j == NU - 1) x = mul_rn(x, we[i + NU * k + 3 * NU2]);
+    else if (k == 0) x = mul_rn(x, we[i + NU * j + 4 * NU2]);
+    else if (k == NU - 1) x = mul_rn(x, we[i + NU * j + 5 * NU2]);
+    us[q] = x;
+  }
+  load_shared(Jt, jht, NU * NV);
+  load_shared(J, jh, NU * NV);
+  __syncthreads();
+  T *ve = v + e * NV3;
+  tensor3_fx<T, NV, NU, xfer_group<NV>()>(us, Jt, J, J, work, work2,
+                                          [&](int q, T val) { ve[q] = val; });
+}
+
+// k_intp_add with NU (coarse) -> NV (fine) fixed
+template <typename T, int NU, int NV>
+__global__ void __launch_bounds__(256) k_intp_fixed(T *out, const T *uc, const T *jh,
+                                                    const T *jht) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T *us = reinterpret_cast<T *>(sm_raw), *work = us + NU * NU * NU, *work2 = work + NV * NU * NU,
+    *J = work2 + NV * NV * NU, *Jt = J + NU * NV;
+  constexpr int NU3 = NU * NU * NU, NV3 = NV * NV * NV;
+  const int e = blockIdx.x;
+  load_shared(us, uc + e * NU3, NU3);
+  load_shared(J, jh, NU * NV);
+  load_shared(Jt, jht, NU * NV);
+  __syncthreads();
+  T *oe = out + e * NV3;
+  tensor3_fx<T, NV, NU, xfer_group<NV>()>(us, J, Jt, Jt, work, work2,
+                                          [&](int q, T val) { oe[q] = add_rn(oe[q], val); });
+}
+
+// The fixed transfer kernels for a (fine, coarse) pair of level sizes:
+// the pairs the default level choice makes for lx1 4..10 and the level
+// lists of the deformed workloads; others take the general kernels.
+template <typename T>
+struct XferFixed {
+  void (*rstr)(T *, const T *, const T *, const T *, const T *) = nullptr;
+  void (*intp)(T *, const T *, const T *, const T *) = nullptr;
+  size_t smem_rstr = 0, smem_intp = 0;
+};
+template <typename T>
+XferFixed<T> xfer_fixed(int nf, int nc) {
+  XferFixed<T> x;
+#define NB_XF(F, C)                                   \
+  if (nf == F && nc == C) {                           \
+    x.rstr = k_rstr_fixed<T, F, C>;                   \
+    x.intp = k_intp_fixed<T, C, F>;                   \
+    x.smem_rstr = xfer_smem<T, F, C>();               \
+    x.smem_intp = xfer_smem<T, C, F>();               \
+    return x;                                         \
+  }
+  NB_XF(3, 2) NB_XF(4, 2) NB_XF(5, 3) NB_XF(6, 2) NB_XF(6, 3) NB_XF(6, 4) NB_XF(7, 4)
+  NB_XF(8, 4) NB_XF(9, 4) NB_XF(10, 4) NB_XF(12, 6) NB_XF(16, 8)
+#undef NB_XF
+  return x;
 }
 
 // set-up helpers -------------------------------------------------------
@@ -338,7 +626,12 @@ __global__ void k_schwarz_wt_setup(double *wt, const double *w, int n, int nelt)
   }
 }
 
-int grid_for(long n) { return int(std::max(1L, std::min<long>(152L * 8, (n + 255) / 256))); }
+template <typename T>
+__global__ void k_sqrt_inplace(T *a, long n) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+       q += long(gridDim.x) * blockDim.x)
+    a[q] = T(sqrt(a[q]));
+}
 
 size_t tensor_smem(int nmax, int extra) {
   return sizeof(double) * (4 * size_t(nmax) * nmax * nmax + extra);
@@ -492,7 +785,7 @@ int overlap_sum(const MgLevel &L, int nelt, double *e, double *B, double *A,
                 cudaStream_t s) {
   k_save_ghost<<<grid_for(L.next), 256, 0, s>>>(A, B, L.nl, nelt);
   NB_TRY(gs_exec(L.gsx, B, 1, 1, 0, s));
-  k_overlap_toreg<double><<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
+  k_overlap_toreg<double><<<line_grid(L.nh, nelt), 256, 0, s>>>(e, B, A, L.nh, nelt);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
@@ -703,6 +996,24 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
   NB_TRY(set_smem((const void *)k_fdm<float>, sm_fdm / 2));
   NB_TRY(set_smem((const void *)k_rstr<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
   NB_TRY(set_smem((const void *)k_intp_add<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
+  for (int l = 2; l <= nlev; ++l) {
+    const int nl = mg->lv[l].nl;
+    if (FdmFn<double> fn = fdm_fixed<double>(nl))
+      NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<double>(nl)));
+    if (FdmFn<float> fn = fdm_fixed<float>(nl))
+      NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<float>(nl)));
+  }
+  for (int l = 1; l < nlev; ++l) {
+    const int nf = mg->lv[l + 1].nh, nc = mg->lv[l].nh;
+    const XferFixed<double> xd = xfer_fixed<double>(nf, nc);
+    const XferFixed<float> xf = xfer_fixed<float>(nf, nc);
+    if (xd.rstr) {
+      NB_TRY(set_smem((const void *)xd.rstr, xd.smem_rstr));
+      NB_TRY(set_smem((const void *)xd.intp, xd.smem_intp));
+      NB_TRY(set_smem((const void *)xf.rstr, xf.smem_rstr));
+      NB_TRY(set_smem((const void *)xf.intp, xf.smem_intp));
+    }
+  }
   if (precision == 32) {
     for (int l = 1; l <= nlev; ++l) {
       MgLevel &L = mg->lv[l];
@@ -723,6 +1034,14 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
     NB_TRY(dmalloc(&mg->A_f, maxext));
     NB_TRY(dmalloc(&mg->B_f, maxext));
     NB_TRY(dmalloc(&mg->z_f, op.n));
+  }
+  // the smoother applies sqrt(wt): taken once here, in the working precision
+  for (int l = 2; l <= nlev; ++l) {
+    MgLevel &L = mg->lv[l];
+    const long nw = long(L.nh) * L.nh * 12 * nelt;
+    k_sqrt_inplace<double><<<grid_for(nw), 256, 0, s>>>(L.schwarz_wt, nw);
+    if (L.schwarz_wt_f) k_sqrt_inplace<float><<<grid_for(nw), 256, 0, s>>>(L.schwarz_wt_f, nw);
+    NB_CUDA(cudaGetLastError());
   }
   NB_CUDA(cudaStreamSynchronize(s));
   return NB_OK;
@@ -770,18 +1089,14 @@ int mg_schwarz(Multigrid &mg, T *e, T *r, int l, cudaStream_t s) {
   const int nelt = mg.op->nelt;
   T *A = V::A(mg), *B = V::B(mg);
   NB_TRY(vec_mask<T>(r, L.mask, L.nmask, s));
-  k_toext<T><<<grid_for(L.next), 256, 0, s>>>(A, r, L.nh, nelt);
+  k_toext<T><<<line_grid(L.nl, nelt), 256, 0, s>>>(A, r, L.nh, nelt);
   NB_TRY(gs_exec(L.gsx, A, V::dom, 1, 0, s));
-  k_ghost_minus<T><<<grid_for(L.next), 256, 0, s>>>(A, L.nh, nelt);
-  const int nl = L.nl;
-  const size_t sm = sizeof(T) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
-  k_fdm<T><<<nelt, 256, sm, s>>>(B, A, V::fast_s(L), V::fast_d(L), nl);
-  NB_CUDA(cudaGetLastError());
+  NB_TRY(launch_fdm<T>(B, A, V::fast_s(L), V::fast_d(L), L.nl, nelt, s));
   NB_TRY(gs_exec(L.gsx, B, V::dom, 1, 0, s));
-  k_overlap_toreg<T><<<grid_for(L.n), 256, 0, s>>>(e, B, A, L.nh, nelt);
+  k_overlap_toreg<T><<<line_grid(L.nh, nelt), 256, 0, s>>>(e, B, A, L.nh, nelt);
   NB_TRY(gs_exec(L.gs, e, V::dom, 1, 0, s));
   NB_TRY(vec_mask<T>(e, L.mask, L.nmask, s));
-  k_schwarz_wt<T><<<grid_for(L.n), 256, 0, s>>>(e, V::schwarz_wt(L), L.nh, nelt);
+  k_schwarz_wt<T><<<line_grid(L.nh, nelt), 256, 0, s>>>(e, V::schwarz_wt(L), L.nh, nelt);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
@@ -790,9 +1105,14 @@ template <typename T>
 int mg_rstr(Multigrid &mg, T *rc, const T *rf, int l, bool dssum, cudaStream_t s) {
   typedef LevelView<T> V;
   const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
-  const int nmax = std::max(F.nh, C.nh);
-  k_rstr<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
-      rc, rf, V::rstr_wt(F), F.nh, C.nh, V::jht(C), V::jh(C));
+  const XferFixed<T> fx = xfer_fixed<T>(F.nh, C.nh);
+  if (fx.rstr) {
+    fx.rstr<<<mg.op->nelt, 256, fx.smem_rstr, s>>>(rc, rf, V::rstr_wt(F), V::jht(C), V::jh(C));
+  } else {
+    const int nmax = std::max(F.nh, C.nh);
+    k_rstr<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
+        rc, rf, V::rstr_wt(F), F.nh, C.nh, V::jht(C), V::jh(C));
+  }
   NB_CUDA(cudaGetLastError());
   if (dssum) NB_TRY(gs_exec(C.gs, rc, V::dom, 1, 0, s));
   return NB_OK;
@@ -802,9 +1122,14 @@ template <typename T>
 int mg_intp_add(Multigrid &mg, T *of, const T *ec, int l, cudaStream_t s) {
   typedef LevelView<T> V;
   const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
-  const int nmax = std::max(F.nh, C.nh);
-  k_intp_add<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
-      of, ec, C.nh, F.nh, V::jh(C), V::jht(C));
+  const XferFixed<T> fx = xfer_fixed<T>(F.nh, C.nh);
+  if (fx.intp) {
+    fx.intp<<<mg.op->nelt, 256, fx.smem_intp, s>>>(of, ec, V::jh(C), V::jht(C));
+  } else {
+    const int nmax = std::max(F.nh, C.nh);
+    k_intp_add<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
+        of, ec, C.nh, F.nh, V::jh(C), V::jht(C));
+  }
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
