@@ -158,6 +158,10 @@ int  nb_mesh_destroy(nb_mesh *mesh);
  * group and member order); 0 on the host with jl's sort-based construction
  * (gs_setup, jl/gs.c:88-113, 330-357).  Both give identical maps. */
 void nb_set_setup_on_device(int on);
+/* hsmg kernels: 1 (default) the FDM and inter-level transfer kernels built
+ * for fixed sizes where one exists, 0 the general kernels only.  Both make
+ * the same sums in the same order (bitwise-equal results). */
+void nb_set_mg_fixed_kernels(int on);
 /* The mesh's gather-scatter groups (jl order: groups by primary, members
  * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)
  * are filled when given. */

@@ -746,6 +746,7 @@ int nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
 }
 
 void nb_set_setup_on_device(int on) { set_setup_on_device(on != 0); }
+void nb_set_mg_fixed_kernels(int on) { mg_set_fixed_kernels(on != 0); }
 
 // Copies one device int array (count entries) to host, when dst is given.
 static int copy_out(void *dst, const void *src, size_t bytes) {

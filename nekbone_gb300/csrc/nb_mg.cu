@@ -183,93 +183,162 @@ __global__ void k_fdm(T *B, T *A, const T *s, const T *d, int nl) {
   }
 }
 
-// The FDM tensor applies with the extended size NL known at compile time:
-// a work item is one 1-D line and a group of G of its outputs (independent
-// multiply-add chains), every loop fully unrolled with constant offsets.
-// Each output is the same left-to-right sum as tensor3's.  Two buffers
-// suffice: the input in X, the passes X -> Y -> X -> Y, the result in Y.
-template <typename T, int NL, int G>
-__device__ __forceinline__ void tensor3_fixed(T *X, T *Y, const T *A, const T *Bt,
-                                              const T *Ct) {
-  constexpr int NG = (NL + G - 1) / G;
-  const int t = threadIdx.x, nt = blockDim.x;
-  for (int it = t; it < NL * NL * NG; it += nt) {  // Y(a, np) = sum_m A(a,m) X(m, np)
-    const int np_ = it / NG, a0 = (it % NG) * G;
-    T x[NL];
+// The FDM kernel with the extended size NL known at compile time.  Each of
+// the six tensor passes is Out(i, j) = sum_k C(i, k) In(k, j) over one
+// element: In is stored [k][j] (slice stride PS, j contiguous), the 1-D
+// matrix as C[k][i] (stride IP, i contiguous), and a thread owns a 4 x 4
+// tile of outputs, so each k step is two 16-byte shared loads for sixteen
+// multiply-adds.  Each pass writes its output already laid out [k'][j'] for
+// the next pass's contraction index k'.  Every output is the left-to-right
+// sum of tensor3 (first term a product, then fused multiply-adds in k
+// order), so the results are bitwise those of the general kernel.
+template <typename T, int NL>
+struct FdmShape {
+  static constexpr int NL2 = NL * NL, NL3 = NL2 * NL;
+  static constexpr int PS = (NL2 + 3) & ~3;  // slice stride of the data buffers
+  static constexpr int IP = (NL + 3) & ~3;   // row stride of the 1-D matrices
+  static constexpr int NIG = IP / 4, NJG = PS / 4, TILES = NIG * NJG;
+  static constexpr int THREADS = (TILES + 31) / 32 * 32;
+  static constexpr size_t SMEM = sizeof(T) * (2 * size_t(NL) * PS + 6 * size_t(NL) * IP);
+};
+
+template <typename T>
+struct Vec4 {
+  T v[4];
+};
+__device__ __forceinline__ Vec4<float> ld4(const float *p) {
+  const float4 a = *reinterpret_cast<const float4 *>(p);
+  return {{a.x, a.y, a.z, a.w}};
+}
+__device__ __forceinline__ Vec4<double> ld4(const double *p) {
+  const double2 a = reinterpret_cast<const double2 *>(p)[0];
+  const double2 b = reinterpret_cast<const double2 *>(p)[1];
+  return {{a.x, a.y, b.x, b.y}};
+}
+
+// one pass; output (i, j) goes to Out[place(j) + i * IS]
+template <typename T, int NL, int IS, typename Place>
+__device__ __forceinline__ void fdm_pass(T *Out, const T *In, const T *C, Place place) {
+  typedef FdmShape<T, NL> F;
+  const int t = threadIdx.x;
+  if (t < F::TILES) {
+    const int i0 = 4 * (t % F::NIG), j0 = 4 * (t / F::NIG);
+    T acc[4][4];
+    {
+      const Vec4<T> c = ld4(C + i0), x = ld4(In + j0);
 #pragma unroll
-    for (int m = 0; m < NL; ++m) x[m] = X[m + np_ * NL];
+      for (int a = 0; a < 4; ++a)
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int a = a0 + g < NL ? a0 + g : NL - 1;
-      T acc = mul_rn(A[a], x[0]);
-#pragma unroll
-      for (int m = 1; m < NL; ++m) acc = fma_rn(A[a + m * NL], x[m], acc);
-      if (a0 + g < NL) Y[a + np_ * NL] = acc;
+        for (int b = 0; b < 4; ++b) acc[a][b] = mul_rn(c.v[a], x.v[b]);
     }
-  }
-  __syncthreads();
-  for (int it = t; it < NL * NL * NG; it += nt) {  // X(a,b,p) = sum_n Y(a,n,p) Bt(n,b)
-    const int ap = it / NG, b0 = (it % NG) * G;
-    const int a = ap % NL, p = ap / NL;
-    const T *wp = Y + NL * NL * p;
-    T x[NL];
 #pragma unroll
-    for (int n = 0; n < NL; ++n) x[n] = wp[a + n * NL];
+    for (int k = 1; k < NL; ++k) {
+      const Vec4<T> c = ld4(C + k * F::IP + i0), x = ld4(In + k * F::PS + j0);
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int b = b0 + g < NL ? b0 + g : NL - 1;
-      T acc = mul_rn(x[0], Bt[b * NL]);
+      for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int n = 1; n < NL; ++n) acc = fma_rn(x[n], Bt[n + b * NL], acc);
-      if (b0 + g < NL) X[a + NL * b + NL * NL * p] = acc;
+        for (int b = 0; b < 4; ++b) acc[a][b] = fma_rn(c.v[a], x.v[b], acc[a][b]);
     }
-  }
-  __syncthreads();
-  for (int it = t; it < NL * NL * NG; it += nt) {  // Y(ab, c) = sum_p X(ab,p) Ct(p,c)
-    const int ab = it / NG, c0 = (it % NG) * G;
-    T x[NL];
 #pragma unroll
-    for (int p = 0; p < NL; ++p) x[p] = X[ab + p * NL * NL];
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + b;
+      if (j >= F::NL2) break;
+      T *o = Out + place(j) + i0 * IS;
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int c = c0 + g < NL ? c0 + g : NL - 1;
-      T acc = mul_rn(x[0], Ct[c * NL]);
-#pragma unroll
-      for (int p = 1; p < NL; ++p) acc = fma_rn(x[p], Ct[p + c * NL], acc);
-      if (c0 + g < NL) Y[ab + NL * NL * c] = acc;
+      for (int a = 0; a < 4; ++a)
+        if (i0 + a < NL) o[a * IS] = acc[a][b];
     }
   }
   __syncthreads();
 }
 
+// [Ct (x) Bt (x) A] applied to X (laid out [a][b + NL c]); the result lands
+// in Y laid out [c][a + NL b].  X is overwritten.
 template <typename T, int NL>
-__global__ void __launch_bounds__(256) k_fdm_fixed(T *B, T *A, const T *s, const T *d) {
+__device__ __forceinline__ void fdm_tensor3(T *X, T *Y, const T *C3) {
+  typedef FdmShape<T, NL> F;
+  constexpr int PS = F::PS, MS = NL * F::IP;
+  // work(a', b + NL c) -> Y[b][a' + NL c]
+  fdm_pass<T, NL, 1>(Y, X, C3, [](int j) { return (j % NL) * PS + NL * (j / NL); });
+  // work2(a', b', c) from Y[b][a' + NL c] -> X[c][a' + NL b']
+  fdm_pass<T, NL, NL>(X, Y, C3 + MS, [](int j) { return (j / NL) * PS + (j % NL); });
+  // v(a', b', c') from X[c][a' + NL b'] -> Y[c'][a' + NL b']
+  fdm_pass<T, NL, PS>(Y, X, C3 + 2 * MS, [](int j) { return j; });
+}
+
+template <typename T, int NL>
+__global__ void __launch_bounds__(FdmShape<T, NL>::THREADS)
+    k_fdm_fixed(T *B, T *A, const T *s, const T *d) {
+  typedef FdmShape<T, NL> F;
+  constexpr int NL2 = F::NL2, NL3 = F::NL3, PS = F::PS, IP = F::IP, MS = NL * IP, HI = NL - 1;
   extern __shared__ __align__(16) unsigned char sm_raw[];
-  T *sm = reinterpret_cast<T *>(sm_raw);
-  constexpr int NL2 = NL * NL, NL3 = NL2 * NL, G = NL >= 8 ? 4 : 2;
-  T *X = sm, *Y = X + NL3, *S = Y + NL3;
-  const int e = blockIdx.x;
-  for (int q = threadIdx.x; q < NL3; q += blockDim.x)
-    X[q] = ghost_minus_at(A + e * NL3, q % NL, (q / NL) % NL, q / NL2, NL);
-  load_shared(S, s + e * 6 * NL2, 6 * NL2);
+  T *X = reinterpret_cast<T *>(sm_raw), *Y = X + NL * PS, *C = Y + NL * PS;
+  const int e = blockIdx.x, nt = blockDim.x;
+  const T *Ae = A + e * NL3, *se = s + e * 6 * NL2, *de = d + e * NL3;
+  // X[a][b + NL c] = A with extrude(A,0,1,A,2,-1) applied: one thread per
+  // (b, c) line, a unrolled.  A ghost-face point (exactly one coordinate on
+  // the ghost layer) takes minus its layer-2 partner: along the line for
+  // a = 0 / NL-1, else in the partner line (b or c moved to 2 / NL-3).
+  for (int t = threadIdx.x; t < NL2; t += nt) {
+    const int b = t % NL, c = t / NL;
+    const bool gb = b == 0 || b == HI, gc = c == 0 || c == HI;
+    const T *line = Ae + NL * t;
+    T v[NL];
+#pragma unroll
+    for (int a = 0; a < NL; ++a) v[a] = line[a];
+    if (!gb && !gc) {
+      v[0] = fma_rn(T(-1), v[2], v[0]);
+      v[HI] = fma_rn(T(-1), v[NL - 3], v[HI]);
+    } else if (gb != gc) {
+      const int pb = gb ? (b == 0 ? 2 : NL - 3) : b, pc = gc ? (c == 0 ? 2 : NL - 3) : c;
+      const T *partner = Ae + NL * (pb + NL * pc);
+#pragma unroll
+      for (int a = 1; a < HI; ++a) v[a] = fma_rn(T(-1), partner[a], v[a]);
+    }
+#pragma unroll
+    for (int a = 0; a < NL; ++a) X[a * PS + t] = v[a];
+  }
+  // the 1-D matrices as C[k][i]: s(1,2,1), s(1,1,2), s(1,1,3) for the first
+  // apply (A, Bt, Ct of tensor3), s(1,1,1), s(1,2,2), s(1,2,3) for the second
+  for (int q = threadIdx.x; q < 6 * MS; q += nt) {
+    const int m = q / MS, r = q - m * MS, k = r / IP, i = r - k * IP;
+    const int src = m == 0 ? 1 : m == 1 ? 2 : m == 2 ? 4 : m == 3 ? 0 : m == 4 ? 3 : 5;
+    const T *S = se + src * NL2;
+    const bool slot_a = m == 0 || m == 3;  // the A slot: C(i,k) = S[i + k NL]
+    C[q] = i < NL ? (slot_a ? S[i + k * NL] : S[k + i * NL]) : T(0);
+  }
   __syncthreads();
-  tensor3_fixed<T, NL, G>(X, Y, S + NL2, S + 2 * NL2, S + 4 * NL2);
-  const T *de = d + e * NL3;
-  for (int q = threadIdx.x; q < NL3; q += blockDim.x) X[q] = mul_rn(de[q], Y[q]);
+  fdm_tensor3<T, NL>(X, Y, C);
+  // d .* v, from Y[c][a + NL b] back to X[a][b + NL c], one (b, c) line each
+  for (int t = threadIdx.x; t < NL2; t += nt) {
+    const int b = t % NL, c = t / NL;
+    const T *yl = Y + c * PS + NL * b, *dl = de + NL * t;
+#pragma unroll
+    for (int a = 0; a < NL; ++a) X[a * PS + t] = mul_rn(dl[a], yl[a]);
+  }
   __syncthreads();
-  tensor3_fixed<T, NL, G>(X, Y, S, S + 3 * NL2, S + 5 * NL2);
-  for (int q = threadIdx.x; q < NL3; q += blockDim.x) {
-    const int a = q % NL, b = (q / NL) % NL, c = q / NL2;
-    B[e * NL3 + q] = Y[q];
-    if (ghost_face(a, b, c, NL)) A[e * NL3 + q] = Y[q];
+  fdm_tensor3<T, NL>(X, Y, C + 3 * MS);
+  // B = v; Y[c][a + NL b] is the natural order with slices PS apart
+  T *Be = B + e * NL3;
+  for (int q = threadIdx.x; q < NL3; q += nt) Be[q] = Y[(q / NL2) * PS + q % NL2];
+  // ghost faces of v into A: face f = 2 axis + side, (x, y) its interior point
+  constexpr int NF = (NL - 2) * (NL - 2);
+  T *Aw = A + e * NL3;
+  for (int q = threadIdx.x; q < 6 * NF; q += nt) {
+    const int f = q / NF, r = q - f * NF, x = r % (NL - 2) + 1, y = r / (NL - 2) + 1;
+    const int g = (f & 1) ? HI : 0;
+    const int a = f < 2 ? g : x, b = f < 2 ? x : (f < 4 ? g : y), c = f < 4 ? y : g;
+    Aw[a + NL * b + NL2 * c] = Y[c * PS + a + NL * b];
   }
 }
+
+bool g_fixed_kernels = true;
 
 // The fixed-size FDM kernel for an extended size nl (5..18), else null
 template <typename T>
 using FdmFn = void (*)(T *, T *, const T *, const T *);
 template <typename T>
-FdmFn<T> fdm_fixed(int nl) {
+FdmFn<T> fdm_fixed_any(int nl) {
   switch (nl) {
 #define NB_FDM(N) \
   case N: return k_fdm_fixed<T, N>;
@@ -279,21 +348,48 @@ FdmFn<T> fdm_fixed(int nl) {
     default: return nullptr;
   }
 }
+template <typename T>
+FdmFn<T> fdm_fixed(int nl) {
+  return g_fixed_kernels ? fdm_fixed_any<T>(nl) : nullptr;
+}
 
 template <typename T>
 size_t fdm_smem(int nl) {
   return sizeof(T) * (4 * size_t(nl) * nl * nl + 6 * nl * nl);
 }
+// shared bytes and threads of the fixed kernel for nl (0 when none)
+template <typename T>
+void fdm_fixed_shape(int nl, size_t *smem, int *threads) {
+  switch (nl) {
+#define NB_FDM(N)                              \
+  case N:                                      \
+    *smem = FdmShape<T, N>::SMEM;              \
+    *threads = FdmShape<T, N>::THREADS;        \
+    return;
+    NB_FDM(5) NB_FDM(6) NB_FDM(7) NB_FDM(8) NB_FDM(9) NB_FDM(10) NB_FDM(11) NB_FDM(12)
+    NB_FDM(13) NB_FDM(14) NB_FDM(15) NB_FDM(16) NB_FDM(17) NB_FDM(18)
+#undef NB_FDM
+    default: *smem = 0, *threads = 0;
+  }
+}
 template <typename T>
 size_t fdm_fixed_smem(int nl) {
-  return sizeof(T) * (2 * size_t(nl) * nl * nl + 6 * nl * nl);
+  size_t sm;
+  int th;
+  fdm_fixed_shape<T>(nl, &sm, &th);
+  return sm;
 }
 
 // FDM launch: the fixed-size kernel where one exists, else the general one
 // (shared-memory limits raised once in the set-up)
 template <typename T>
 int launch_fdm(T *B, T *A, const T *s, const T *d, int nl, int nelt, cudaStream_t st) {
-  if (FdmFn<T> fn = fdm_fixed<T>(nl)) fn<<<nelt, 256, fdm_fixed_smem<T>(nl), st>>>(B, A, s, d);
+  if (FdmFn<T> fn = fdm_fixed<T>(nl)) {
+    size_t sm;
+    int th;
+    fdm_fixed_shape<T>(nl, &sm, &th);
+    fn<<<nelt, th, sm, st>>>(B, A, s, d);
+  }
   else k_fdm<T><<<nelt, 256, fdm_smem<T>(nl), st>>>(B, A, s, d, nl);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
@@ -549,7 +645,7 @@ struct XferFixed {
   size_t smem_rstr = 0, smem_intp = 0;
 };
 template <typename T>
-XferFixed<T> xfer_fixed(int nf, int nc) {
+XferFixed<T> xfer_fixed_any(int nf, int nc) {
   XferFixed<T> x;
 #define NB_XF(F, C)                                   \
   if (nf == F && nc == C) {                           \
@@ -563,6 +659,10 @@ XferFixed<T> xfer_fixed(int nf, int nc) {
   NB_XF(8, 4) NB_XF(9, 4) NB_XF(10, 4) NB_XF(12, 6) NB_XF(16, 8)
 #undef NB_XF
   return x;
+}
+template <typename T>
+XferFixed<T> xfer_fixed(int nf, int nc) {
+  return g_fixed_kernels ? xfer_fixed_any<T>(nf, nc) : XferFixed<T>();
 }
 
 // set-up helpers -------------------------------------------------------
@@ -998,15 +1098,15 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
   NB_TRY(set_smem((const void *)k_intp_add<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
   for (int l = 2; l <= nlev; ++l) {
     const int nl = mg->lv[l].nl;
-    if (FdmFn<double> fn = fdm_fixed<double>(nl))
+    if (FdmFn<double> fn = fdm_fixed_any<double>(nl))
       NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<double>(nl)));
-    if (FdmFn<float> fn = fdm_fixed<float>(nl))
+    if (FdmFn<float> fn = fdm_fixed_any<float>(nl))
       NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<float>(nl)));
   }
   for (int l = 1; l < nlev; ++l) {
     const int nf = mg->lv[l + 1].nh, nc = mg->lv[l].nh;
-    const XferFixed<double> xd = xfer_fixed<double>(nf, nc);
-    const XferFixed<float> xf = xfer_fixed<float>(nf, nc);
+    const XferFixed<double> xd = xfer_fixed_any<double>(nf, nc);
+    const XferFixed<float> xf = xfer_fixed_any<float>(nf, nc);
     if (xd.rstr) {
       NB_TRY(set_smem((const void *)xd.rstr, xd.smem_rstr));
       NB_TRY(set_smem((const void *)xd.intp, xd.smem_intp));
@@ -1218,6 +1318,8 @@ int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
 }
 
 }  // namespace
+
+void mg_set_fixed_kernels(bool on) { g_fixed_kernels = on; }
 
 // R A P of the V-cycle's transfers on a level-1 vector x1 (local copies):
 // the result r1 is assembled (dssum) and masked, as the coarse step sees it.

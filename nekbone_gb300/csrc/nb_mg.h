@@ -59,6 +59,8 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
 // kMaxCoarse unknowns.
 constexpr int kMaxCoarse = 16384;
 int mg_setup_coarse(Multigrid *mg, const double *g, cudaStream_t s);
+// the fixed-size FDM and transfer kernels (default) or the general ones only
+void mg_set_fixed_kernels(bool on);
 // h1mg_solve (hsmg.f:960-1034): z = M^-1 rhs; masks rhs in place.
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s);
 

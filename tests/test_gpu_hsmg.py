@@ -120,3 +120,26 @@ def test_exact_coarse_is_galerkin(torch):
     m.mg_solve(z.data_ptr(), f.clone().data_ptr())
     torch.cuda.synchronize()
     assert torch.isfinite(z).all()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("levels", [[2, 5, 11], [1, 3, 7, 11]])
+def test_fixed_size_kernels_bitwise(torch, precision, levels):
+    """The fixed-size FDM and transfer kernels make the general kernels'
+    sums in the same order: one V-cycle is bitwise the same either way."""
+    import nekbone_gb300 as nb
+    m, g, c, f = _setup(torch, 4, 12, deformed=True)
+    out = {}
+    try:
+        for fixed in (True, False):
+            nb.set_mg_fixed_kernels(fixed)
+            m.mg_setup(levels, precision=precision)
+            rhs = f.clone()
+            z = torch.zeros_like(f)
+            m.mg_solve(z.data_ptr(), rhs.data_ptr())
+            torch.cuda.synchronize()
+            out[fixed] = z.cpu().numpy()
+    finally:
+        nb.set_mg_fixed_kernels(True)
+    assert np.abs(out[True]).max() > 0
+    assert np.array_equal(out[True], out[False])
