@@ -429,48 +429,29 @@ __global__ void k_overlap_toreg(T *e_out, const T *B, const T *A, int nh, int ne
   }
 }
 
-// h1mg_schwarz_wt3d2 (hsmg.f:1144-1178): e *= sqrt(wt), three sweeps over
-// the layers L = {0, 1, n-2, n-1}: x faces, then y faces of the x-interior,
-// then z faces of the x- and y-interior.  A point takes the factors of
-// every layer slot s it sits in, in slot order (two slots coincide when
-// n < 4).  wt holds sqrt(wt), taken once at set-up in precision T.
+// Layer slots of coordinate x in an n-point line: bit s set when x sits in
+// slot s of L = {0, 1, n-2, n-1}.
+__device__ __forceinline__ int wt_slots(int x, int n) {
+  return (x == 0) | (x == 1) << 1 | (x == n - 2) << 2 | (x == n - 1) << 3;
+}
+// h1mg_schwarz_wt3d2 (hsmg.f:1144-1178) at point (i, j, k) of an element:
+// x *= sqrt(wt) over three sweeps of the layers L: x faces, then y faces of
+// the x-interior, then z faces of the x- and y-interior.  A point takes the
+// factor of every slot it sits in, in slot order (two slots coincide when
+// n < 4).  we: the element's 12 n^2 weights, square-rooted at set-up.
 template <typename T>
-__global__ void k_schwarz_wt(T *e, const T *wt, int n, int nelt) {
-  const int n2 = n * n, lines = n2 * nelt;
-  // bit s set: x sits in layer slot s
-  auto slots = [&](int x) {
-    return (x == 0) | (x == 1) << 1 | (x == n - 2) << 2 | (x == n - 1) << 3;
-  };
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < lines; t += gridDim.x * blockDim.x) {
-    const int el = t / n2, ij = t - el * n2, i = ij % n, j = ij / n;
-    const int mi = slots(i), mj = slots(j);
-    // the sweep that owns the line's points (z: decided per point) and the
-    // face-array offset of its (a, b) pair
-    const int dir = mi ? 0 : mj ? 1 : 2;
-    const int m_line = mi ? mi : mj;
-    const T *we = wt + el * 12 * n2 + 4 * n2 * dir + (dir == 2 ? i + n * j : (dir == 1 ? i : j));
-    const int kstride = dir == 2 ? 0 : n;  // W(.,k,...) steps with k in sweeps 0 and 1
-    T *ee = e + el * n2 * n + ij;
-    for (int k0 = 0; k0 < n; k0 += kChunk) {
-      T v[kChunk];
-      int m[kChunk];
+__device__ __forceinline__ T schwarz_weigh(T x, const T *we, int n, int i, int j, int k) {
+  const int n2 = n * n, mi = wt_slots(i, n), mj = wt_slots(j, n);
+  const T *w;
+  int m;
+  if (mi) w = we + j + n * k, m = mi;
+  else if (mj) w = we + 4 * n2 + i + n * k, m = mj;
+  else if ((m = wt_slots(k, n))) w = we + 8 * n2 + i + n * j;
+  else return x;
 #pragma unroll
-      for (int u = 0; u < kChunk; ++u) {
-        const int k = k0 + u;
-        m[u] = k < n ? (dir == 2 ? slots(k) : m_line) : 0;
-        if (!m[u]) continue;
-        T x = ee[k * n2];
-        const T *wk = we + k * kstride;
-#pragma unroll
-        for (int sl = 0; sl < 4; ++sl)
-          if (m[u] >> sl & 1) x = mul_rn(x, wk[sl * n2]);
-        v[u] = x;
-      }
-#pragma unroll
-      for (int u = 0; u < kChunk; ++u)
-        if (m[u]) ee[(k0 + u) * n2] = v[u];
-    }
-  }
+  for (int sl = 0; sl < 4; ++sl)
+    if (m >> sl & 1) x = mul_rn(x, w[sl * n2]);
+  return x;
 }
 
 // h1mg_rstr (hsmg.f:1340-1360): do_wt (hsmg.f:1362-1391) then
@@ -504,9 +485,13 @@ __global__ void k_rstr(T *v, const T *u, const T *wt, int nu, int nv, const T *j
   for (int q = threadIdx.x; q < nv3; q += blockDim.x) v[e * nv3 + q] = vs[q];
 }
 
-// h1mg_intp (hsmg.f:1436-1475) accumulated: out += [J (x) J (x) J] uc
+// h1mg_intp (hsmg.f:1436-1475) accumulated: out += [J (x) J (x) J] uc.
+// With wt (the fine level's square-rooted Schwarz weights), out is first
+// weighted as h1mg_schwarz_wt3d2 would have left it: the smoother's last
+// pass, fused into the one kernel that reads its output next.
 template <typename T>
-__global__ void k_intp_add(T *out, const T *uc, int nu, int nv, const T *jh, const T *jht) {
+__global__ void k_intp_add(T *out, const T *uc, int nu, int nv, const T *jh, const T *jht,
+                           const T *wt) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *sm = reinterpret_cast<T *>(sm_raw);
   const int nmax = max(nu, nv), nmax3 = nmax * nmax * nmax;
@@ -519,8 +504,12 @@ __global__ void k_intp_add(T *out, const T *uc, int nu, int nv, const T *jh, con
   load_shared(Jt, jht, nu * nv);
   __syncthreads();
   tensor3<T>(vs, us, nv, nu, J, Jt, Jt, work, work2);
-  for (int q = threadIdx.x; q < nv3; q += blockDim.x)
-    out[e * nv3 + q] = add_rn(out[e * nv3 + q], vs[q]);
+  const T *we = wt ? wt + e * 12 * nv * nv : nullptr;
+  for (int q = threadIdx.x; q < nv3; q += blockDim.x) {
+    T o = out[e * nv3 + q];
+    if (we) o = schwarz_weigh(o, we, nv, q % nv, (q / nv) % nv, q / (nv * nv));
+    out[e * nv3 + q] = add_rn(o, vs[q]);
+  }
 }
 
 // Inter-level transfers with both sizes known at compile time: NU input
@@ -620,7 +609,7 @@ __global__ void __launch_bounds__(256) k_rstr_fixed(T *v, const T *u, const T *w
 // k_intp_add with NU (coarse) -> NV (fine) fixed
 template <typename T, int NU, int NV>
 __global__ void __launch_bounds__(256) k_intp_fixed(T *out, const T *uc, const T *jh,
-                                                    const T *jht) {
+                                                    const T *jht, const T *wt) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T *us = reinterpret_cast<T *>(sm_raw), *work = us + NU * NU * NU, *work2 = work + NV * NU * NU,
     *J = work2 + NV * NV * NU, *Jt = J + NU * NV;
@@ -630,9 +619,19 @@ __global__ void __launch_bounds__(256) k_intp_fixed(T *out, const T *uc, const T
   load_shared(J, jh, NU * NV);
   load_shared(Jt, jht, NU * NV);
   __syncthreads();
-  T *oe = out + e * NV3;
+  // the interpolant into shared memory, then one coalesced
+  // read-modify-write of out
+  T *vs = Jt + NU * NV;
   tensor3_fx<T, NV, NU, xfer_group<NV>()>(us, J, Jt, Jt, work, work2,
-                                          [&](int q, T val) { oe[q] = add_rn(oe[q], val); });
+                                          [&](int q, T val) { vs[q] = val; });
+  __syncthreads();
+  T *oe = out + e * NV3;
+  const T *we = wt ? wt + e * 12 * NV * NV : nullptr;
+  for (int q = threadIdx.x; q < NV3; q += blockDim.x) {
+    T o = oe[q];
+    if (we) o = schwarz_weigh(o, we, NV, q % NV, (q / NV) % NV, q / (NV * NV));
+    oe[q] = add_rn(o, vs[q]);
+  }
 }
 
 // The fixed transfer kernels for a (fine, coarse) pair of level sizes:
@@ -641,19 +640,19 @@ __global__ void __launch_bounds__(256) k_intp_fixed(T *out, const T *uc, const T
 template <typename T>
 struct XferFixed {
   void (*rstr)(T *, const T *, const T *, const T *, const T *) = nullptr;
-  void (*intp)(T *, const T *, const T *, const T *) = nullptr;
+  void (*intp)(T *, const T *, const T *, const T *, const T *) = nullptr;
   size_t smem_rstr = 0, smem_intp = 0;
 };
 template <typename T>
 XferFixed<T> xfer_fixed_any(int nf, int nc) {
   XferFixed<T> x;
-#define NB_XF(F, C)                                   \
-  if (nf == F && nc == C) {                           \
-    x.rstr = k_rstr_fixed<T, F, C>;                   \
-    x.intp = k_intp_fixed<T, C, F>;                   \
-    x.smem_rstr = xfer_smem<T, F, C>();               \
-    x.smem_intp = xfer_smem<T, C, F>();               \
-    return x;                                         \
+#define NB_XF(F, C)                                              \
+  if (nf == F && nc == C) {                                      \
+    x.rstr = k_rstr_fixed<T, F, C>;                              \
+    x.intp = k_intp_fixed<T, C, F>;                              \
+    x.smem_rstr = xfer_smem<T, F, C>();                          \
+    x.smem_intp = xfer_smem<T, C, F>() + sizeof(T) * F * F * F;  \
+    return x;                                                    \
   }
   NB_XF(3, 2) NB_XF(4, 2) NB_XF(5, 3) NB_XF(6, 2) NB_XF(6, 3) NB_XF(6, 4) NB_XF(7, 4)
   NB_XF(8, 4) NB_XF(9, 4) NB_XF(10, 4) NB_XF(12, 6) NB_XF(16, 8)
@@ -1181,7 +1180,9 @@ struct LevelView<float> {
   static constexpr int dom = 2;
 };
 
-// h1mg_schwarz (hsmg.f:1036-1051) at level l: e = sqrt(W) part1(r); masks r
+// h1mg_schwarz (hsmg.f:1036-1051) at level l: e = part1(r), masked; masks
+// r.  The final e *= sqrt(W) (h1mg_schwarz_wt) is left to the interpolation
+// that next reads e (mg_intp_add with weigh), which applies it on its load.
 template <typename T>
 int mg_schwarz(Multigrid &mg, T *e, T *r, int l, cudaStream_t s) {
   typedef LevelView<T> V;
@@ -1196,7 +1197,6 @@ int mg_schwarz(Multigrid &mg, T *e, T *r, int l, cudaStream_t s) {
   k_overlap_toreg<T><<<line_grid(L.nh, nelt), 256, 0, s>>>(e, B, A, L.nh, nelt);
   NB_TRY(gs_exec(L.gs, e, V::dom, 1, 0, s));
   NB_TRY(vec_mask<T>(e, L.mask, L.nmask, s));
-  k_schwarz_wt<T><<<line_grid(L.nh, nelt), 256, 0, s>>>(e, V::schwarz_wt(L), L.nh, nelt);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
@@ -1218,17 +1218,20 @@ int mg_rstr(Multigrid &mg, T *rc, const T *rf, int l, bool dssum, cudaStream_t s
   return NB_OK;
 }
 
+// of += J ec from level l to l+1; weigh: first apply level l+1's Schwarz
+// weights to of (the smoother's output there)
 template <typename T>
-int mg_intp_add(Multigrid &mg, T *of, const T *ec, int l, cudaStream_t s) {
+int mg_intp_add(Multigrid &mg, T *of, const T *ec, int l, bool weigh, cudaStream_t s) {
   typedef LevelView<T> V;
   const MgLevel &F = mg.lv[l + 1], &C = mg.lv[l];
+  const T *wt = weigh ? V::schwarz_wt(F) : nullptr;
   const XferFixed<T> fx = xfer_fixed<T>(F.nh, C.nh);
   if (fx.intp) {
-    fx.intp<<<mg.op->nelt, 256, fx.smem_intp, s>>>(of, ec, V::jh(C), V::jht(C));
+    fx.intp<<<mg.op->nelt, 256, fx.smem_intp, s>>>(of, ec, V::jh(C), V::jht(C), wt);
   } else {
     const int nmax = std::max(F.nh, C.nh);
     k_intp_add<T><<<mg.op->nelt, 256, tensor_smem(nmax, 2 * F.nh * C.nh) * sizeof(T) / 8, s>>>(
-        of, ec, C.nh, F.nh, V::jh(C), V::jht(C));
+        of, ec, C.nh, F.nh, V::jh(C), V::jht(C), wt);
   }
   NB_CUDA(cudaGetLastError());
   return NB_OK;
@@ -1313,8 +1316,8 @@ int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
     NB_CUDA(cudaGetLastError());
   }
   for (int l = 2; l <= Lm - 1; ++l)
-    NB_TRY(mg_intp_add<T>(mg, V::e(mg.lv[l]), V::e(mg.lv[l - 1]), l - 1, s));
-  return mg_intp_add<T>(mg, zT, V::e(mg.lv[Lm - 1]), Lm - 1, s);
+    NB_TRY(mg_intp_add<T>(mg, V::e(mg.lv[l]), V::e(mg.lv[l - 1]), l - 1, true, s));
+  return mg_intp_add<T>(mg, zT, V::e(mg.lv[Lm - 1]), Lm - 1, true, s);
 }
 
 }  // namespace
@@ -1331,11 +1334,11 @@ static int coarse_rap(Multigrid &mg, const double *g, double *x1, double *z, dou
   const double *src = x1;
   for (int l = 2; l < L; ++l) {
     NB_CUDA(cudaMemsetAsync(mg.lv[l].e, 0, mg.lv[l].n * sizeof(double), s));
-    NB_TRY(mg_intp_add<double>(mg, mg.lv[l].e, src, l - 1, s));
+    NB_TRY(mg_intp_add<double>(mg, mg.lv[l].e, src, l - 1, false, s));
     src = mg.lv[l].e;
   }
   NB_CUDA(cudaMemsetAsync(z, 0, op.n * sizeof(double), s));
-  NB_TRY(mg_intp_add<double>(mg, z, src, L - 1, s));
+  NB_TRY(mg_intp_add<double>(mg, z, src, L - 1, false, s));
   // A
   NB_TRY(apply_ax<double>(op, w, z, g, s));
   // R: the downward leg, masked at every level as h1mg_schwarz masks r
