@@ -65,9 +65,9 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-sample-nel", type=int, default=16)
     ap.add_argument("--cpu-sample-iters", type=int, default=250)
-    ap.add_argument("--case", choices=["cg", "tc", "batch"], default="cg",
-                    help="cg: the benchmark; tc / batch: a small case of the tensor-core "
-                         "operator / the batched solver, for profiling")
+    ap.add_argument("--case", choices=["cg", "tc", "batch", "hsmg"], default="cg",
+                    help="cg: the benchmark; tc / batch / hsmg: a small case of the "
+                         "tensor-core operator / the batched solver / hsmg PCG, for profiling")
     return ap.parse_args()
 
 
@@ -546,7 +546,9 @@ def run_case(a):
     """Small cases for kernel profiles (one JSON line of timings, not a bench
     line): 'tc' applies the tensor-core and CUDA-core FP32 operators on 16^3
     deformed elements (lx1 = --lx); 'batch' solves the first 32 problems of
-    the batched workload once after tuning."""
+    the batched workload once after tuning; 'hsmg' runs 6 PCG iterations with
+    the FP32-smoother V-cycle (levels 12 -> 6 -> 2 points, exact coarse solve)
+    on 16^3 deformed elements, lx1 = 12."""
     import torch
     import nekbone_gb300 as nb
     dev = torch.device("cuda", 0)
@@ -566,6 +568,25 @@ def run_case(a):
                                                                 g32.data_ptr()), reps=3),
                "fp32_ms": _time_on(stream, torch, lambda: m.ax_f32(w.data_ptr(), u.data_ptr(),
                                                                    g32.data_ptr()), reps=3)}
+    elif a.case == "hsmg":
+        m = nb.DeviceMesh(16, 16, 16, 12, mask_mode=1)
+        n = m.n
+        g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+        c = torch.empty(n, dtype=torch.float64, device=dev)
+        f = torch.empty(n, dtype=torch.float64, device=dev)
+        m.setup_g_deformed(g.data_ptr(), 11, 0.1)
+        m.set_multiplicity(c.data_ptr())
+        m.rhs_uniform(f.data_ptr(), c.data_ptr(), 5)
+        m.mg_setup([1, 5, 11], precision=32)
+        m.mg_setup_coarse(g.data_ptr())
+        x = torch.zeros_like(f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it, rr = m.pcg_tol(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), 1e-10,
+                           max_iter=6, check_every=6)
+        out = {"case": "hsmg", "n": n, "iters": it, "relres": rr,
+               "s": time.perf_counter() - t0}
+        m.close()
     else:
         b = nb.Batch(batch_boxes()[:32])
         b.setup(777)

@@ -1097,10 +1097,17 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
   NB_TRY(set_smem((const void *)k_intp_add<float>, tensor_smem(maxnl, 2 * maxnl * maxnl) / 2));
   for (int l = 2; l <= nlev; ++l) {
     const int nl = mg->lv[l].nl;
-    if (FdmFn<double> fn = fdm_fixed_any<double>(nl))
+    // the whole unified L1 as shared memory: occupancy is shared-memory bound
+    if (FdmFn<double> fn = fdm_fixed_any<double>(nl)) {
       NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<double>(nl)));
-    if (FdmFn<float> fn = fdm_fixed_any<float>(nl))
+      NB_CUDA(cudaFuncSetAttribute((const void *)fn,
+                                   cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
+    if (FdmFn<float> fn = fdm_fixed_any<float>(nl)) {
       NB_TRY(set_smem((const void *)fn, fdm_fixed_smem<float>(nl)));
+      NB_CUDA(cudaFuncSetAttribute((const void *)fn,
+                                   cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    }
   }
   for (int l = 1; l < nlev; ++l) {
     const int nf = mg->lv[l + 1].nh, nc = mg->lv[l].nh;
