@@ -162,6 +162,11 @@ void nb_set_setup_on_device(int on);
  * for fixed sizes where one exists, 0 the general kernels only.  Both make
  * the same sums in the same order (bitwise-equal results). */
 void nb_set_mg_fixed_kernels(int on);
+/* Mixed solver: 1 (default) when every element's FP32 metric block equals
+ * element 0's (a box of equal elements, as setup_g makes), the inner
+ * operator reads that one block instead of each element's; 0 always reads
+ * each element's.  Same values either way (bitwise-equal results). */
+void nb_set_shared_metric(int on);
 /* The mesh's gather-scatter groups (jl order: groups by primary, members
  * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)
  * are filled when given. */

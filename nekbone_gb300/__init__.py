@@ -53,7 +53,7 @@ EXPORTS = (
     "nb_batch_create", "nb_batch_destroy", "nb_batch_info", "nb_batch_problem",
     "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
-    "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_mesh_gs_maps",
+    "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse",
 )
@@ -122,6 +122,8 @@ lib.nb_set_setup_on_device.restype = None
 lib.nb_set_setup_on_device.argtypes = [_i]
 lib.nb_set_mg_fixed_kernels.restype = None
 lib.nb_set_mg_fixed_kernels.argtypes = [_i]
+lib.nb_set_shared_metric.restype = None
+lib.nb_set_shared_metric.argtypes = [_i]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
@@ -608,6 +610,12 @@ def set_setup_on_device(on: bool) -> None:
 def set_mg_fixed_kernels(on: bool) -> None:
     """hsmg: fixed-size FDM/transfer kernels (default) or the general ones."""
     lib.nb_set_mg_fixed_kernels(1 if on else 0)
+
+
+def set_shared_metric(on: bool) -> None:
+    """Mixed solver: one shared FP32 metric block when all elements' are
+    equal (default), or always each element's."""
+    lib.nb_set_shared_metric(1 if on else 0)
 
 
 def tc_selftest(bf16: bool = False) -> int:

@@ -20,11 +20,13 @@ int launch_ax_eo_shape(AxArgs<T> a, const T *eo, cudaStream_t s) {
   return NB_OK;
 }
 
-// FP32 with a 16-byte aligned metric: the bulk-copy (TMAG) form
+// FP32 with a 16-byte aligned per-element metric: the bulk-copy (TMAG)
+// form.  A shared metric block (g_uniform) is read directly: it stays
+// cache-resident, and without the copy's shared memory more CTAs fit.
 template <typename T, int LX, int MODE>
 int launch_ax_eo_lx(AxArgs<T> a, const T *eo, cudaStream_t s) {
   if constexpr (sizeof(T) == 4 && MODE != 2 && (24 * LX * LX * LX) % 16 == 0) {
-    if ((reinterpret_cast<uintptr_t>(a.g) & 15u) == 0)
+    if (!a.g_uniform && (reinterpret_cast<uintptr_t>(a.g) & 15u) == 0)
       return launch_ax_eo_shape<T, LX, MODE, true>(a, eo, s);
   }
   return launch_ax_eo_shape<T, LX, MODE, false>(a, eo, s);

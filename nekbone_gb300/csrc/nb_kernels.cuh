@@ -117,6 +117,7 @@ struct AxArgs {
   const float *e;    // MODE 2: FP32 correction added to x first (may be null)
   double scale;      // MODE 2: its scale
   unsigned *err;     // device error word for bounded waits (may be null)
+  int g_uniform;     // every element's metric block equals element 0's: read that one
 };
 
 template <typename T, int LX>
@@ -790,11 +791,13 @@ __global__ void __launch_bounds__(LX * LX)
   const int i = threadIdx.x, j = threadIdx.y;  // own column (i,j)
   const int e = blockIdx.x;
   const size_t base = size_t(e) * L3;
+  // the element's metric block (the shared one when all blocks are equal)
+  const T *gblk = a.g + (a.g_uniform ? size_t(0) : 6 * base);
   if (TMAG && t == 0) {
     constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));
     mbar_init(&sm.bar, 1);
     mbar_arrive_expect_tx(&sm.bar, GBYTES);
-    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
+    bulk_g2s(sm.g, gblk, GBYTES, &sm.bar);
   }
   const T *Ed = sm.E4, *Od = sm.E4 + H * H;            // of D
   const T *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;  // of D^T
@@ -865,10 +868,9 @@ __global__ void __launch_bounds__(LX * LX)
   for (int k = 0; k < LX; ++k) {
     const int q = eo_at<LX>(i, j, k);
     const T ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
-    const size_t pt = base + size_t(k) * L2 + t;
     typedef typename Vec2<T>::type V2;
     const V2 *gp = TMAG ? reinterpret_cast<const V2 *>(&sm.g[6 * (k * L2 + t)])
-                        : reinterpret_cast<const V2 *>(a.g + 6 * pt);
+                        : reinterpret_cast<const V2 *>(gblk + 6 * (k * L2 + t));
     const V2 g01 = gp[0], g23 = gp[1], g45 = gp[2];
     T wr = mul_rn(g01.x, ur);
     wr = fma_rn(g01.y, us, wr);

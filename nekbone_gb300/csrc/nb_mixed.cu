@@ -4,6 +4,7 @@
 // no counterpart for these solvers (its cg runs a fixed niter, cg.f:48-75);
 // they reuse the same operator, numbering, mask and norm
 // sqrt(r'Cr) (cg.f:42,66-69).
+#include <algorithm>
 #include <cmath>
 #include <memory>
 #include <vector>
@@ -180,6 +181,56 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
   return NB_OK;
 }
 
+}  // extern "C"
+
+namespace nb {
+namespace {
+// *same = 0 if any element's metric block (blk values) differs bitwise from
+// element 0's: x indexes the block, y strides over elements 1..nelt-1
+__global__ void k_metric_uniform(const unsigned *g, long blk, long nelt, int *same) {
+  const long q = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  bool ok = true;
+  if (q < blk) {
+    const unsigned v = g[q];
+    for (long e = 1 + blockIdx.y; e < nelt; e += gridDim.y) ok &= g[e * blk + q] == v;
+  }
+  if (!__syncthreads_and(ok) && threadIdx.x == 0) atomicExch(same, 0);
+}
+}  // namespace
+
+// Whether every element of the FP32 metric g32 repeats element 0's block
+// (a box of equal affine elements: the reference's own setup_g).  Then the
+// element operator reads one cache-resident block instead of 24 B per point,
+// with the same values, so the same results.
+bool g_shared_metric = true;
+void set_shared_metric(bool on) { g_shared_metric = on; }
+
+// flag: one device int of scratch
+int metric_uniform(const float *g32, long nelt, int lx, int *flag, int *uniform,
+                   cudaStream_t s) {
+  const long blk = 6L * lx * lx * lx;
+  const int one = 1;
+  int h = 0;
+  *uniform = 0;
+  if (!g_shared_metric) return NB_OK;
+  NB_CUDA(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  if (nelt > 1) {
+    const dim3 grid(unsigned((blk + 255) / 256), unsigned(std::min<long>(nelt - 1, 1024)));
+    k_metric_uniform<<<grid, 256, 0, s>>>(reinterpret_cast<const unsigned *>(g32), blk, nelt,
+                                          flag);
+    NB_CUDA(cudaGetLastError());
+  }
+  NB_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NB_CUDA(cudaStreamSynchronize(s));
+  *uniform = h;
+  return NB_OK;
+}
+}  // namespace nb
+
+extern "C" {
+
+void nb_set_shared_metric(int on) { set_shared_metric(on != 0); }
+
 int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
                 const double *c, double tol, int inner_iters, int max_outer,
                 int *outer, int *inner_total, double *relres) {
@@ -190,8 +241,10 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   CgWork &wk = *static_cast<CgWork *>(pwk);
   cudaStream_t s = lib_stream();
   const long n = op.n;
-  // scratch: r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32 (FP32)
-  int st = wk.ensure_scratch(size_t(n) * (2 * 8 + 12 * 4));
+  // reduction buffers (this may be the mesh's first solve), then scratch:
+  // r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32 (FP32); one int flag
+  int st = wk.ensure(op, std::max(inner_iters, 1));
+  if (!st) st = wk.ensure_scratch(size_t(n) * (2 * 8 + 12 * 4) + 16);
   if (st) return st;
   double *r = reinterpret_cast<double *>(wk.scratch);
   double *w = r + n;
@@ -202,6 +255,9 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   double rn0 = 0.0, rn = 0.0;
   if (!st) st = vec_convert<float, double>(g32, g, 6 * n, s);
   if (!st) st = vec_convert<float, double>(c32, c, n, s);
+  int uniform = 0;
+  int *flag = reinterpret_cast<int *>(wk.scratch + size_t(n) * (2 * 8 + 12 * 4));
+  if (!st) st = metric_uniform(g32, op.nelt, op.lx, flag, &uniform, s);
   // x = 0, r = mask(f)
   if (!st && cudaMemsetAsync(x, 0, n * 8, s) != cudaSuccess) st = fail(NB_ERR_CUDA, "memset");
   if (!st) st = vec_copy<double>(r, f, n, s);
@@ -221,7 +277,9 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     if (rn0 == 0.0 || rn / rn0 <= tol || k >= max_outer) break;
     // inner FP32 solve of A e = r / |r|
     st = dev_scale_to_f32(r32, r, 1.0 / rn, n, s);
+    wk.g32_uniform = uniform;
     if (!st) st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s);
+    wk.g32_uniform = 0;
     // FP64 defect: x += |r| e; r = f - A x; r'Cr
     if (!st && fused) {
       st = residual_fused(op, wk, x, e32, rn, f, g, c, r, w, s);

@@ -520,6 +520,7 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
       a.sc = wk.sc;
       a.partial = wk.partial_ax;
       a.first = iter == 1;
+      a.g_uniform = std::is_same<T, float>::value ? wk.g32_uniform : 0;
       NB_TRY(launch_ax<T>(op, 1, a, s));
       k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx,
                                              op.nbg, wk.partial_gs, wk.partial_ax,

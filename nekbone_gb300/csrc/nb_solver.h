@@ -62,6 +62,9 @@ struct CgWork {
   // repeated solve allocates nothing)
   unsigned char *scratch = nullptr;
   size_t scratch_bytes = 0;
+  // the FP32 metric of the solve in progress has one block for all
+  // elements (set by the mixed solver around its inner CG)
+  int g32_uniform = 0;
   ~CgWork();
   int ensure(const Operator &op, int niter);
   int ensure_scratch(size_t bytes);

@@ -248,6 +248,40 @@ def test_fp32_and_mixed_precision(nb):
     assert np.allclose(h32[:, 0], h64[:, 0], rtol=1e-3)
 
 
+@pytest.mark.parametrize("deformed", [False, True])
+def test_mixed_shared_metric_bitwise(nb, deformed):
+    """The mixed solver's shared FP32 metric block (all elements equal, as
+    setup_g makes them) gives bitwise the solution of per-element reads."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(6, 5, 4, 10, mask_mode=1)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    if deformed:
+        m.setup_g_deformed(g.data_ptr(), 3, 0.1)
+    else:
+        m.setup_g(g.data_ptr())
+        blk = g.view(-1, 6 * 10 ** 3)
+        assert bool((blk == blk[0]).all())     # the box's blocks repeat
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 11)
+    xs = {}
+    try:
+        for shared in (True, False):
+            nb.set_shared_metric(shared)
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            outer, inner, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(),
+                                          c.data_ptr(), 1e-10, 20)
+            assert rr <= 1e-10
+            xs[shared] = (x.cpu().numpy(), outer)
+    finally:
+        nb.set_shared_metric(True)
+    assert xs[True][1] == xs[False][1]
+    assert np.array_equal(xs[True][0], xs[False][0])
+
+
 # -------------------------------------------------------------------- hsmg --
 @pytest.mark.parametrize("nx", [4, 5, 8, 10])
 def test_h1mg_solve_matches_oracle(nb, nx):
