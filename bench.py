@@ -149,6 +149,19 @@ def cpu_rate(nel: int, lx: int, iters: int, threads: int):
     return ctx.n * iters / dt / 1e9, dt, ctx.n
 
 
+def replica_rate(ms, n, niter, steps, world, device=None):
+    """Whole-job rate of `world` independent replicas (one mesh of n points
+    per rank, niter iterations per step): every rank's work over the slowest
+    rank's time.  Returns (max ms over ranks, GDOF*iter/s)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * n * niter * steps / (ms / 1e3) / 1e9
+
+
 def run_reference(a, rank, world):
     if rank != 0:
         return
@@ -419,14 +432,9 @@ def run_ours(a, rank, world, local):
         e1.synchronize()
     nb.sync()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_rate(e0.elapsed_time(e1), n, niter, a.steps, world, dev)
     clocks = clk.summary()
     ms_per_step = ms / a.steps
-    value = world * n * niter * a.steps / (ms / 1e3) / 1e9
     launches_per_step = 2 + 3 * niter  # copy/mask/glsc3 + 3 kernels per iteration
 
     # dominant kernel timing (the fused element operator) on the same stream
