@@ -544,6 +544,13 @@ def run_ours(a, rank, world, local):
         out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                "sample": f"{a.cpu_sample_nel}^3 elements, lx1={lx} (n={ns}), "
                                          f"{a.cpu_sample_iters} FP64 CG iterations, {dt:.1f} s"}
+        # the same port on one core (the reference has no threading of its own)
+        it1 = max(2, a.cpu_sample_iters // threads)
+        v1, dt1, _ = cpu_rate(a.cpu_sample_nel, lx, it1, 1)
+        out["cpu_baseline_single_core"] = {
+            "value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{a.cpu_sample_nel}^3 elements, lx1={lx} (n={ns}), {it1} FP64 CG "
+                      f"iterations, {dt1:.1f} s"}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
