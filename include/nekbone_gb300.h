@@ -153,10 +153,12 @@ typedef struct nb_mesh nb_mesh;
 int  nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
                     int mask_mode);
 int  nb_mesh_destroy(nb_mesh *mesh);
-/* Where nb_mesh_create builds a full-mask mesh's topology: 1 (default) on
- * the device, without a sort (closed-form copies of each box point, jl's
- * group and member order); 0 on the host with jl's sort-based construction
- * (gs_setup, jl/gs.c:88-113, 330-357).  Both give identical maps. */
+/* Where box topologies are built: 1 (default) on the device, without a sort
+ * (closed-form copies of each box point, jl's group and member order); 0 on
+ * the host with jl's sort-based construction (gs_setup, jl/gs.c:88-113,
+ * 330-357).  Both give identical maps.  It covers nb_mesh_create and
+ * gs_setup_, which recognises set_vert_box's numbering of a brick box (a
+ * device check of every point) and otherwise sorts on the host. */
 void nb_set_setup_on_device(int on);
 /* hsmg kernels: 1 (default) the FDM and inter-level transfer kernels built
  * for fixed sizes where one exists, 0 the general kernels only.  Both make

@@ -15,6 +15,8 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "../../include/nekbone_gb300.h"
@@ -72,9 +74,23 @@ void set_error_mode(int m) { g_mode = m; }
 
 // ----------------------------------------------------------- global state --
 struct GsEntry {
-  GsHost host;
+  GsHost host;           // jl's maps; empty for a recognised box until needed
   GsDevice dev;
   int n = 0;
+  // set_vert_box's numbering of a brick box, recognised by gs_setup_: the
+  // maps were built on the device without a sort
+  bool box = false;
+  int lx = 0, nelx = 0, nely = 0, nelz = 0;
+  int ensure_host() {
+    if (!box || !host.map[0].empty()) return NB_OK;
+    const long nelt = long(nelx) * nely * nelz;
+    std::vector<int> lglel(nelt);
+    for (long e = 0; e < nelt; ++e) lglel[e] = int(e + 1);
+    std::vector<int64_t> glo(n);
+    set_vert_box(glo.data(), lx, int(nelt), nelx, nely, lglel.data());
+    gs_topology(glo.data(), n, &host);
+    return NB_OK;
+  }
 };
 
 struct DevBuf {
@@ -154,8 +170,18 @@ int common_op(Operator **out) {
     if (g->n != n)
       return fail(NB_ERR_ARG, "gsh has %d points, the mesh has %ld", g->n, n);
     std::unique_ptr<Operator> op(new Operator());
-    NB_TRY(operator_from(op.get(), S.nelx, S.nely, S.nelz, S.nelt, S.nx1,
-                         S.lglel.data(), S.dxm1.data(), g->host, S.mask_mode, S.s));
+    bool brick = g->box && g->lx == S.nx1 && g->nelx == S.nelx && g->nely == S.nely &&
+                 g->nelz == S.nelz && setup_on_device();
+    for (int e = 0; brick && e < S.nelt; ++e) brick = S.lglel[e] == e + 1;
+    if (brick) {  // the box's topology on the device, as nb_mesh_create builds it
+      NB_TRY(operator_base(op.get(), S.nelx, S.nely, S.nelz, S.nelt, S.nx1, S.lglel.data(),
+                           S.dxm1.data(), S.mask_mode, S.s));
+      NB_TRY(box_topology_device(op.get(), S.s));
+    } else {
+      NB_TRY(g->ensure_host());
+      NB_TRY(operator_from(op.get(), S.nelx, S.nely, S.nelz, S.nelt, S.nx1,
+                           S.lglel.data(), S.dxm1.data(), g->host, S.mask_mode, S.s));
+    }
     op->order = S.order;
     S.op = std::move(op);
   }
@@ -297,8 +323,17 @@ void gs_setup_(int *handle, const int64_t *glo_num, const int *n,
   }
   std::unique_ptr<GsEntry> e(new GsEntry());
   e->n = *n;
-  gs_topology(glo_num, *n, &e->host);
-  if (gs_upload(e->host, *n, &e->dev, S.s)) return;
+  bool box = false;
+  if (setup_on_device() &&
+      box_numbering(glo_num, *n, &box, &e->lx, &e->nelx, &e->nely, &e->nelz, S.s))
+    return;
+  if (box) {  // no sort: the closed-form copies of each box point
+    e->box = true;
+    if (box_gs_device(e->lx, e->nelx, e->nely, e->nelz, &e->dev, S.s)) return;
+  } else {
+    gs_topology(glo_num, *n, &e->host);
+    if (gs_upload(e->host, *n, &e->dev, S.s)) return;
+  }
   S.gs.push_back(std::move(e));
   *handle = int(S.gs.size()) - 1;
 }
@@ -686,6 +721,22 @@ void set_vert_box_(int64_t *glo_num, const int *nx) {
   set_vert_box(glo_num, *nx, S.nelt, S.nelx, S.nely, S.lglel.data());
 }
 
+// body(lo, hi) over [0, n) split across the host's threads: the set-up
+// loops below compute every entry on its own, so the split changes nothing
+extern "C++" {
+template <typename F>
+static void host_parallel(long n, F body) {
+  const long nt = std::max(1L, std::min<long>(std::thread::hardware_concurrency(), n / 65536));
+  if (nt == 1) {
+    body(0L, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (long t = 0; t < nt; ++t) th.emplace_back(body, n * t / nt, n * (t + 1) / nt);
+  for (auto &x : th) x.join();
+}
+}
+
 void setup_g_(double *g) {
   clear_status();
   State &S = st();
@@ -693,19 +744,19 @@ void setup_g_(double *g) {
   const int lx = S.nx1;
   std::vector<double> a(lx * lx), b(lx), c(lx * lx), d(lx * lx), z(lx);
   semhat(a.data(), b.data(), c.data(), d.data(), z.data(), lx - 1);
-  long p = 0;
-  for (int e = 0; e < S.nelt; ++e)
-    for (int k = 0; k < lx; ++k)
-      for (int j = 0; j < lx; ++j)
-        for (int i = 0; i < lx; ++i, ++p) {
-          double *gp = g + 6 * p;
-          const double v = b[i] * b[j] * b[k];
-          gp[0] = v;
-          gp[1] = gp[2] = 0.;
-          gp[3] = v;
-          gp[4] = 0.;
-          gp[5] = v;
-        }
+  const long l3 = long(lx) * lx * lx;
+  host_parallel(long(S.nelt) * l3, [&](long lo, long hi) {
+    for (long p = lo; p < hi; ++p) {
+      const int r = int(p % l3), i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+      double *gp = g + 6 * p;
+      const double v = b[i] * b[j] * b[k];
+      gp[0] = v;
+      gp[1] = gp[2] = 0.;
+      gp[3] = v;
+      gp[4] = 0.;
+      gp[5] = v;
+    }
+  });
 }
 
 void set_multiplicity_(double *c) {
@@ -722,11 +773,14 @@ void set_multiplicity_(double *c) {
 
 void set_f_(double *f, const double *c, const int *n) {
   clear_status();
-  for (int i = 1; i <= *n; ++i) {
-    double arg = 1.e9 * double(wrap_mul(i, i));
-    arg = 1.e9 * std::cos(arg);
-    f[i - 1] = std::sin(arg);
-  }
+  host_parallel(*n, [&](long lo, long hi) {
+    for (long q = lo; q < hi; ++q) {
+      const int i = int(q + 1);
+      double arg = 1.e9 * double(wrap_mul(i, i));
+      arg = 1.e9 * std::cos(arg);
+      f[q] = std::sin(arg);
+    }
+  });
   dssum_(f);
   if (last_status()) return;
   for (int i = 0; i < *n; ++i) f[i] = f[i] * c[i];

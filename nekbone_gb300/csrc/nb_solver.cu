@@ -172,8 +172,27 @@ static void build_boundary_groups(Operator *op) {
   }
   op->bnd_off_h.push_back(int(op->bnd_idx_h.size()));
   op->nbg = int(op->bnd_off_h.size()) - 1;
+  op->nbnd = long(op->bnd_idx_h.size());
   op->fused_ok = n < (1L << 31);
 }
+
+namespace {
+// Mask flags of boundary-group members built on the device: bit 31 set
+// exactly for the members in the sorted list (binary search).
+__global__ void k_set_member_flags(unsigned *idx, long nm, const int *list, int nl) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < nm;
+       q += long(gridDim.x) * blockDim.x) {
+    const unsigned id = idx[q] & 0x7fffffffu;
+    int lo = 0, hi = nl;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (unsigned(list[mid]) < id) lo = mid + 1;
+      else hi = mid;
+    }
+    idx[q] = id | (lo < nl && unsigned(list[lo]) == id ? 0x80000000u : 0u);
+  }
+}
+}  // namespace
 
 std::vector<int> full_mask_list(const Operator &op) {
   std::vector<int> list;
@@ -207,7 +226,16 @@ int operator_set_mask(Operator *op, const std::vector<int> &list_in) {
     NB_CUDA(cudaMemcpy(op->d_mask_list, list.data(), list.size() * sizeof(int),
                        cudaMemcpyHostToDevice));
   }
-  if (op->nbg > 0 && !op->bnd_idx_h.empty()) {
+  if (op->nbg > 0 && op->bnd_idx_h.empty() && op->bnd_idx) {
+    // groups built on the device (nb_topo.cu): flags set there
+    for (int v : list)
+      if (!is_elem_boundary(v, op->lx)) op->fused_ok = false;
+    k_set_member_flags<<<int(std::max(1L, std::min<long>(152L * 8, (op->nbnd + 255) / 256))),
+                         256, 0, op->stream>>>(op->bnd_idx, op->nbnd, op->d_mask_list,
+                                               op->n_mask);
+    NB_CUDA(cudaGetLastError());
+    NB_CUDA(cudaStreamSynchronize(op->stream));
+  } else if (op->nbg > 0 && !op->bnd_idx_h.empty()) {
     for (int v : list)
       if (!is_elem_boundary(v, op->lx)) op->fused_ok = false;
     std::vector<unsigned char> masked(op->n, 0);
@@ -298,7 +326,7 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
   for (long e = 0; e < nelt; ++e) lglel[e] = int(e + 1);  // brick, np=1
   std::vector<double> a(lx * lx), b(lx), c(lx * lx), d(lx * lx), z(lx);
   semhat(a.data(), b.data(), c.data(), d.data(), z.data(), lx - 1);
-  if (mask_mode == 1 && setup_on_device()) {
+  if (setup_on_device()) {
     NB_TRY(operator_base(op, nelx, nely, nelz, int(nelt), lx, lglel.data(), d.data(),
                          mask_mode, s));
     return box_topology_device(op, s);

@@ -38,6 +38,7 @@ struct Operator {
   // fused gather-scatter over element boundary points
   bool fused_ok = false;
   int nbg = 0;
+  long nbnd = 0;                    // members over all boundary groups
   std::vector<int> bnd_off_h;
   std::vector<unsigned> bnd_idx_h;  // without mask flags
   int *bnd_off = nullptr;
@@ -86,11 +87,18 @@ bool even_odd_tables(const std::vector<double> &D, int lx, std::vector<double> &
 // its even-odd tables, the domain faces of every element.
 int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
                   const int *lglel, const double *dxm1, int mask_mode, cudaStream_t s);
-// The gather-scatter groups, the fused boundary groups with their mask flags
-// and the full Dirichlet mask list of a brick-ordered box, built on the
-// device without a sort (nb_topo.cu).  The host jl maps stay empty until
-// ensure_host_maps builds them.
+// The gather-scatter groups and the fused boundary groups of a brick-ordered
+// box, built on the device without a sort (nb_topo.cu).  Mask mode 1 also
+// gets the full Dirichlet mask list and the members' mask flags; mode 0
+// starts unmasked (maskit builds its list on first use).  The host jl maps
+// stay empty until ensure_host_maps builds them.
 int box_topology_device(Operator *op, cudaStream_t s);
+// Whether glo_num (n points) is set_vert_box's numbering of a box in the
+// brick element order (lglel(e) = e): the sizes are read off the first
+// points, then every point is checked on the device.  On success *lx,
+// *nelx, *nely, *nelz hold the box.
+int box_numbering(const int64_t *glo_num, long n, bool *is_box, int *lx, int *nelx,
+                  int *nely, int *nelz, cudaStream_t s);
 // The gather-scatter CSR alone for lx points per element direction on the
 // same brick (the multigrid levels' regular and extended numberings).
 int box_gs_device(int lx, int nelx, int nely, int nelz, GsDevice *g, cudaStream_t s);

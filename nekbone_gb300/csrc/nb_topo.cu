@@ -18,6 +18,7 @@
 //   * the fused pass's boundary groups: every element-boundary point's group,
 //     singletons included, members on a domain face flagged in bit 31;
 //   * the full Dirichlet mask list (every element's domain-face points).
+#include <algorithm>
 #include <vector>
 
 #include "nb_solver.h"
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(1024) k_topo_scan(int *blocksum, int nb, long 
 
 __global__ void __launch_bounds__(kThr)
     k_topo_emit(Box b, const int *blockpre, int *gs_off, int *gs_idx, int *bd_off,
-                unsigned *bd_idx, int *mask) {
+                unsigned *bd_idx, int *mask, bool flags) {
   const long q0 = long(blockIdx.x) * kBlk + long(threadIdx.x) * kPts;
   int v[5] = {0, 0, 0, 0, 0};
   for (int p = 0; p < kPts; ++p) {
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(kThr)
     if (bd_off && pi.primary && pi.boundary) {
       bd_off[pos[2]] = pos[3];
       for (int k = 0; k < pi.m; ++k)
-        bd_idx[pos[3] + k] = unsigned(pi.q[k]) | (pi.masked ? 0x80000000u : 0u);
+        bd_idx[pos[3] + k] = unsigned(pi.q[k]) | (flags && pi.masked ? 0x80000000u : 0u);
       pos[2] += 1;
       pos[3] += pi.m;
     }
@@ -209,7 +210,7 @@ void set_setup_on_device(bool on) { g_setup_on_device = on; }
 namespace {
 
 // The sweep for lx points per element direction; bnd/mask outputs are
-// produced only when op is given.
+// produced only when op is given, the mask list and flags for mask mode 1.
 int topology_sweep(const Box &b, GsDevice *g, Operator *op, cudaStream_t s) {
   if (b.n >= (1L << 31))
     return fail(NB_ERR_UNSUPPORTED, "device topology: n = %ld exceeds 2^31-1", b.n);
@@ -236,15 +237,18 @@ int topology_sweep(const Box &b, GsDevice *g, Operator *op, cudaStream_t s) {
   g->ng = int(tot[0]);
   NB_CUDA(cudaMalloc(&g->off, (tot[0] + 1) * sizeof(int)));
   NB_CUDA(cudaMalloc(&g->idx, std::max(1L, tot[1]) * sizeof(int)));
+  const bool full = op && op->mask_mode == 1;
   if (op) {
     op->nbg = int(tot[2]);
-    op->n_mask = int(tot[4]);
+    op->nbnd = tot[3];
+    op->n_mask = full ? int(tot[4]) : 0;
     NB_CUDA(cudaMalloc(&op->bnd_off, (tot[2] + 1) * sizeof(int)));
     NB_CUDA(cudaMalloc(&op->bnd_idx, std::max(1L, tot[3]) * sizeof(unsigned)));
-    NB_CUDA(cudaMalloc(&op->d_mask_list, std::max(1L, tot[4]) * sizeof(int)));
+    if (full) NB_CUDA(cudaMalloc(&op->d_mask_list, std::max(1L, tot[4]) * sizeof(int)));
   }
   k_topo_emit<<<nb, kThr, 0, s>>>(b, blocksum, g->off, g->idx, op ? op->bnd_off : nullptr,
-                                  op ? op->bnd_idx : nullptr, op ? op->d_mask_list : nullptr);
+                                  op ? op->bnd_idx : nullptr,
+                                  full ? op->d_mask_list : nullptr, full);
   const int end_gs = int(tot[1]), end_bd = int(tot[3]);
   NB_CUDA(cudaMemcpyAsync(g->off + tot[0], &end_gs, sizeof(int), cudaMemcpyHostToDevice, s));
   if (op)
@@ -264,8 +268,75 @@ int box_topology_device(Operator *op, cudaStream_t s) {
   const Box b{op->lx, op->nelx, op->nely, op->nelz, op->n};
   NB_TRY(topology_sweep(b, &op->gs, op, s));
   op->fused_ok = true;
-  op->mask_built = true;
+  op->mask_built = op->mask_mode == 1;
   op->brick = true;
+  return NB_OK;
+}
+
+namespace {
+// *bad = 1 where glo[q] differs from set_vert_box's value (prox_dssum.f:42-73)
+// for the brick box b
+__global__ void k_box_numbering(Box b, const long long *glo, int *bad) {
+  const int lx = b.lx, nn = lx - 1;
+  const long l3 = long(lx) * lx * lx;
+  const long long ax = (long long)nn * b.nelx + 1, ay = (long long)nn * b.nely + 1;
+  bool ok = true;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < b.n;
+       q += long(gridDim.x) * blockDim.x) {
+    const long e = q / l3;
+    const int r = int(q - e * l3);
+    const int i = r % lx, j = (r / lx) % lx, k = r / (lx * lx);
+    const long long ex = e % b.nelx, ey = (e / b.nelx) % b.nely, ez = e / (long(b.nelx) * b.nely);
+    const long long v = 1 + (nn * ex + i) + (nn * ey + j) * ax + (nn * ez + k) * ax * ay;
+    ok &= glo[q] == v;
+  }
+  if (!__syncthreads_and(ok) && threadIdx.x == 0) atomicExch(bad, 1);
+}
+}  // namespace
+
+int box_numbering(const int64_t *glo, long n, bool *is_box, int *lx_out, int *nelx_out,
+                  int *nely_out, int *nelz_out, cudaStream_t s) {
+  *is_box = false;
+  // glo = q + 1 along element 0's first line; the line ends at q = lx
+  long lx = 0;
+  while (lx < n && lx < 64 && glo[lx] == lx + 1) ++lx;
+  if (lx < 2 || lx >= 64) return NB_OK;
+  const long l3 = lx * lx * lx;
+  if (n < l3 || n % l3) return NB_OK;
+  const long nn = lx - 1, nelt = n / l3;
+  const long ax = glo[lx] - 1;                       // j = 1: 1 + ax
+  if (ax < lx || (ax - 1) % nn) return NB_OK;
+  const long nelx = (ax - 1) / nn;
+  const long axy = glo[lx * lx] - 1;                 // k = 1: 1 + ax*ay
+  if (axy < ax || axy % ax) return NB_OK;
+  const long ay = axy / ax;
+  if ((ay - 1) % nn) return NB_OK;
+  const long nely = (ay - 1) / nn;
+  if (nelx < 1 || nely < 1 || nelt % (nelx * nely)) return NB_OK;
+  const long nelz = nelt / (nelx * nely);
+  if (n >= (1L << 31)) return NB_OK;
+  const Box b{int(lx), int(nelx), int(nely), int(nelz), n};
+  long long *dglo = nullptr;
+  int *bad = nullptr;
+  NB_CUDA(cudaMalloc(&dglo, n * sizeof(long long)));
+  cudaError_t e = cudaMalloc(&bad, sizeof(int));
+  int hb = 1;
+  if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dglo, glo, n * sizeof(long long), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    k_box_numbering<<<int(std::min<long>(152L * 8, (n + 255) / 256)), 256, 0, s>>>(b, dglo, bad);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(dglo);
+  if (bad) cudaFree(bad);
+  if (e != cudaSuccess) return fail(NB_ERR_CUDA, "box_numbering: %s", cudaGetErrorString(e));
+  if (!hb) {
+    *is_box = true;
+    *lx_out = int(lx), *nelx_out = int(nelx), *nely_out = int(nely), *nelz_out = int(nelz);
+  }
   return NB_OK;
 }
 
