@@ -754,32 +754,6 @@ int upload(T **p, const std::vector<T> &h) {
   return NB_OK;
 }
 
-// host gather-scatter sum (jl semantics) for set-up quantities
-void gs_host_add(const GsHost &g, double *u) {
-  const uint32_t END = uint32_t(-1);
-  auto gather = [&](const std::vector<uint32_t> &m) {
-    size_t p = 0;
-    while (m[p] != END) {
-      const uint32_t i = m[p++];
-      double t = u[i];
-      while (m[p] != END) t += u[m[p++]];
-      ++p;
-      u[i] = t;
-    }
-  };
-  auto scatter = [&](const std::vector<uint32_t> &m) {
-    size_t p = 0;
-    while (m[p] != END) {
-      const uint32_t i = m[p++];
-      while (m[p] != END) u[m[p++]] = u[i];
-      ++p;
-    }
-  };
-  gather(g.map[0]);
-  for (size_t q = 0; q + 1 < g.map[2].size(); ++q) u[g.map[2][q]] = 0.0;
-  scatter(g.map[1]);
-}
-
 // h1mg_setup_fast1d_a / _b (hsmg.f:403-481); a, b are (n+3)^2 column-major
 void fast1d_ab(double *a, double *b, int lbc, int rbc, double ll, double lm,
                double lr, const double *ah, const double *bh, int n) {
@@ -1015,8 +989,21 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
       at(2, 2, 1, e) = lm;
       at(2, 2, lx, e) = lm;
     }
-    NB_TRY(ensure_host_maps(const_cast<Operator &>(op)));
-    gs_host_add(op.gsh_host, lw.data());
+    {  // dssum on the device maps (jl's sum order, bitwise the host's)
+      double *d = nullptr;
+      NB_CUDA(cudaMalloc(&d, op.n * sizeof(double)));
+      int st = NB_OK;
+      if (cudaMemcpyAsync(d, lw.data(), op.n * sizeof(double), cudaMemcpyHostToDevice, s) !=
+          cudaSuccess)
+        st = fail(NB_ERR_CUDA, "h1mg_setup: lengths upload");
+      if (!st) st = gs_exec(op.gs, d, 1, 1, 0, s);
+      if (!st && (cudaMemcpyAsync(lw.data(), d, op.n * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s) != cudaSuccess ||
+                  cudaStreamSynchronize(s) != cudaSuccess))
+        st = fail(NB_ERR_CUDA, "h1mg_setup: lengths download");
+      cudaFree(d);
+      NB_TRY(st);
+    }
     for (int l = 2; l <= nlev; ++l) {
       MgLevel &L = mg->lv[l];
       const int nl = L.nl, n = L.order;

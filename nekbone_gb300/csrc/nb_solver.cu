@@ -342,14 +342,6 @@ int operator_box(Operator *op, int nelx, int nely, int nelz, int lx,
   return NB_OK;
 }
 
-int ensure_host_maps(Operator &op) {
-  if (!op.gsh_host.map[0].empty()) return NB_OK;
-  std::vector<int64_t> glo(op.n);
-  set_vert_box(glo.data(), op.lx, op.nelt, op.nelx, op.nely, op.lglel.data());
-  gs_topology(glo.data(), int(op.n), &op.gsh_host);
-  return NB_OK;
-}
-
 // ------------------------------------------------------- vector kernels --
 namespace {
 

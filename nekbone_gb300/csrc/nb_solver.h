@@ -91,7 +91,8 @@ int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
 // box, built on the device without a sort (nb_topo.cu).  Mask mode 1 also
 // gets the full Dirichlet mask list and the members' mask flags; mode 0
 // starts unmasked (maskit builds its list on first use).  The host jl maps
-// stay empty until ensure_host_maps builds them.
+// stay empty: every later use (gather-scatter, multigrid set-up) runs on
+// the device maps.
 int box_topology_device(Operator *op, cudaStream_t s);
 // Whether glo_num (n points) is set_vert_box's numbering of a box in the
 // brick element order (lglel(e) = e): the sizes are read off the first
@@ -102,7 +103,6 @@ int box_numbering(const int64_t *glo_num, long n, bool *is_box, int *lx, int *ne
 // The gather-scatter CSR alone for lx points per element direction on the
 // same brick (the multigrid levels' regular and extended numberings).
 int box_gs_device(int lx, int nelx, int nely, int nelz, GsDevice *g, cudaStream_t s);
-int ensure_host_maps(Operator &op);
 // Whether operator_box builds full-mask topologies on the device (default
 // on); the host path (jl's sort-based construction) stays available.
 bool setup_on_device();

@@ -78,7 +78,8 @@ def test_cg_identical_on_both_topologies(nb):
 
 
 def test_multigrid_on_device_topology(nb):
-    """hsmg builds its host maps on demand when the mesh came from the device."""
+    """hsmg set-up on a device-built mesh (its dssum on the device maps, no
+    host maps at all) gives the host-built mesh's V-cycle, bit for bit."""
     torch = pytest.importorskip("torch")
     res = []
     for device in (True, False):
