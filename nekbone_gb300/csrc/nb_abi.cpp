@@ -218,6 +218,13 @@ struct MgPrecond : Precond {
   int apply(double *z, double *r, cudaStream_t s) override {
     return mg_solve(*mg, z, r, s);
   }
+  // FP32 smoother on a fully masked CG (mask mode 1: r is already zero
+  // wherever the finest level masks, so the in-place mask of r is a no-op)
+  float *r32_in() override {
+    return mg->precision == 32 && mg->op->mask_mode == 1 ? mg->lv[mg->nlev].r_f : nullptr;
+  }
+  int apply_f32(cudaStream_t s) override { return mg_solve_f32(*mg, s); }
+  const float *z32_out() override { return mg->z_f; }
 };
 
 cudaStream_t lib_stream() {

@@ -490,7 +490,8 @@ __global__ void __launch_bounds__(256)
     k_cg_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
                 const T *__restrict__ w, const T *__restrict__ c, long n,
                 double *__restrict__ partial, unsigned *counter, CgScalars *sc,
-                double *hist, int iter, int identity_precond) {
+                double *hist, int iter, int identity_precond,
+                float *__restrict__ r32 = nullptr) {
   __shared__ double red[32];
   const T alpha = T(sc->alpha);
   const T alphm = -alpha;
@@ -500,6 +501,7 @@ __global__ void __launch_bounds__(256)
     x[q] = fma_rn(alpha, p[q], x[q]);
     const T rv = fma_rn(alphm, w[q], r[q]);
     r[q] = rv;
+    if (r32) r32[q] = float(rv);  // the FP32 V-cycle's input, as k_to_f32 makes it
     part = fma_rn(mul_rn(rv, c[q]), rv, part);
   }
   const double s = block_sum<T>(part, red);
@@ -531,18 +533,29 @@ __global__ void __launch_bounds__(256)
 // ------------------------------------------------------------ reductions --
 // s = glsc3(a,b,mult) (math.f:603-617) into *out via partials; optional
 // CG bookkeeping: mode 1 = initial rnorm (cg.f:42), mode 2 = rtz1 and beta of
-// a preconditioned iteration (cg.f:51-55).
+// a preconditioned iteration (cg.f:51-55).  With mf, the third vector is
+// formed here from the FP32 vector mf (T(mf[q]), as k_to_f64 makes it) and
+// stored to mout (m itself is not read).
 template <typename T>
 __global__ void __launch_bounds__(256)
     k_glsc3(const T *__restrict__ a, const T *__restrict__ b,
-            const T *__restrict__ m, long n, double *__restrict__ partial,
+            const T *m, long n, double *__restrict__ partial,
             unsigned *counter, double *out, CgScalars *sc, int mode,
-            double *hist, int iter) {
+            double *hist, int iter, const float *__restrict__ mf = nullptr,
+            T *mout = nullptr) {
   __shared__ double red[32];
   T part = T(0);
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
-       q += long(gridDim.x) * blockDim.x)
-    part = fma_rn(mul_rn(a[q], b[q]), m[q], part);
+       q += long(gridDim.x) * blockDim.x) {
+    T mv;
+    if (mf) {
+      mv = T(mf[q]);
+      mout[q] = mv;
+    } else {
+      mv = m[q];
+    }
+    part = fma_rn(mul_rn(a[q], b[q]), mv, part);
+  }
   const double s = block_sum<T>(part, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
   if (last_block(counter, gridDim.x)) {

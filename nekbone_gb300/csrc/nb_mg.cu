@@ -47,6 +47,13 @@ Multigrid::~Multigrid() {
   if (c_prim) cudaFree(c_prim);
   if (c_b) cudaFree(c_b);
   if (c_x) cudaFree(c_x);
+  if (A2) cudaFree(A2);
+  if (B2) cudaFree(B2);
+  if (A2_f) cudaFree(A2_f);
+  if (B2_f) cudaFree(B2_f);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (s2) cudaStreamDestroy(s2);
 }
 
 namespace {
@@ -962,6 +969,20 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
   NB_TRY(dmalloc(&mg->A, maxext));
   NB_TRY(dmalloc(&mg->B, maxext));
   NB_TRY(dmalloc(&mg->w, op.n));
+  // work arrays of the second stream's smoothers (levels 2..nlev-1)
+  long lowext = 0;
+  for (int l = 2; l < nlev; ++l)
+    lowext = std::max(lowext, long(mg->lv[l].nh + 2) * (mg->lv[l].nh + 2) *
+                                  (mg->lv[l].nh + 2) * nelt);
+  if (lowext > 0 && precision == 64) {
+    NB_TRY(dmalloc(&mg->A2, lowext));
+    NB_TRY(dmalloc(&mg->B2, lowext));
+  }
+  if (!mg->s2) {
+    NB_CUDA(cudaStreamCreateWithFlags(&mg->s2, cudaStreamNonBlocking));
+    NB_CUDA(cudaEventCreateWithFlags(&mg->ev_fork, cudaEventDisableTiming));
+    NB_CUDA(cudaEventCreateWithFlags(&mg->ev_join, cudaEventDisableTiming));
+  }
   // restriction weights
   for (int l = 1; l <= nlev; ++l) {
     MgLevel &L = mg->lv[l];
@@ -1127,6 +1148,10 @@ int mg_setup(Multigrid *mg, const Operator &op, const int *orders, int nlev,
     NB_TRY(dmalloc(&mg->A_f, maxext));
     NB_TRY(dmalloc(&mg->B_f, maxext));
     NB_TRY(dmalloc(&mg->z_f, op.n));
+    if (lowext > 0) {
+      NB_TRY(dmalloc(&mg->A2_f, lowext));
+      NB_TRY(dmalloc(&mg->B2_f, lowext));
+    }
   }
   // the smoother applies sqrt(wt): taken once here, in the working precision
   for (int l = 2; l <= nlev; ++l) {
@@ -1157,6 +1182,8 @@ struct LevelView<double> {
   static double *r(MgLevel &L) { return L.r; }
   static double *A(Multigrid &m) { return m.A; }
   static double *B(Multigrid &m) { return m.B; }
+  static double *A2(Multigrid &m) { return m.A2; }
+  static double *B2(Multigrid &m) { return m.B2; }
   static constexpr int dom = 1;
 };
 template <>
@@ -1171,19 +1198,22 @@ struct LevelView<float> {
   static float *r(MgLevel &L) { return L.r_f; }
   static float *A(Multigrid &m) { return m.A_f; }
   static float *B(Multigrid &m) { return m.B_f; }
+  static float *A2(Multigrid &m) { return m.A2_f; }
+  static float *B2(Multigrid &m) { return m.B2_f; }
   static constexpr int dom = 2;
 };
 
 // h1mg_schwarz (hsmg.f:1036-1051) at level l: e = part1(r), masked; masks
-// r.  The final e *= sqrt(W) (h1mg_schwarz_wt) is left to the interpolation
-// that next reads e (mg_intp_add with weigh), which applies it on its load.
+// r first when mask_r (the finest level's r is masked by the caller).  The
+// final e *= sqrt(W) (h1mg_schwarz_wt) is left to the interpolation that
+// next reads e (mg_intp_add with weigh), which applies it on its load.
+// A, B: extended work arrays of the stream s.
 template <typename T>
-int mg_schwarz(Multigrid &mg, T *e, T *r, int l, cudaStream_t s) {
+int mg_schwarz(Multigrid &mg, T *e, T *r, int l, T *A, T *B, bool mask_r, cudaStream_t s) {
   typedef LevelView<T> V;
   MgLevel &L = mg.lv[l];
   const int nelt = mg.op->nelt;
-  T *A = V::A(mg), *B = V::B(mg);
-  NB_TRY(vec_mask<T>(r, L.mask, L.nmask, s));
+  if (mask_r) NB_TRY(vec_mask<T>(r, L.mask, L.nmask, s));
   k_toext<T><<<line_grid(L.nl, nelt), 256, 0, s>>>(A, r, L.nh, nelt);
   NB_TRY(gs_exec(L.gsx, A, V::dom, 1, 0, s));
   NB_TRY(launch_fdm<T>(B, A, V::fast_s(L), V::fast_d(L), L.nl, nelt, s));
@@ -1277,40 +1307,55 @@ int coarse_apply(Multigrid &mg, cudaStream_t s) {
 
 // The V-cycle of h1mg_solve (hsmg.f:960-1034) in precision T from level Lm
 // down; the coarse "solve" (copy + dssum + mask, hsmg.f:945-957) is always
-// FP64.  rT is the top-level right-hand side (already masked), zT the result.
+// FP64.  rT is the top-level right-hand side, zT the result.
+//
+// The cycle is additive: every level's Schwarz step reads only its own
+// restricted residual, and the corrections meet on the way up.  So after
+// the finest r is masked, the finest smoother runs on s while the
+// restrictions, the coarser smoothers, the coarse solve and the
+// interpolations up to level Lm-1 run on the second stream s2 (with their
+// own work arrays); s waits for them before the last interpolation.  Each
+// kernel computes what it did in one stream.
 template <typename T>
 int vcycle(Multigrid &mg, T *zT, T *rT, cudaStream_t s) {
   typedef LevelView<T> V;
   const int Lm = mg.nlev;
   MgLevel &Top = mg.lv[Lm];
-  NB_TRY(mg_schwarz<T>(mg, zT, rT, Lm, s));
+  NB_TRY(vec_mask<T>(rT, Top.mask, Top.nmask, s));
   T *rTop = V::r(Top);
   if (rTop != rT) NB_TRY(vec_copy<T>(rTop, rT, Top.n, s));
+  NB_CUDA(cudaEventRecord(mg.ev_fork, s));
+  NB_TRY(mg_schwarz<T>(mg, zT, rT, Lm, V::A(mg), V::B(mg), false, s));
+  cudaStream_t s2 = mg.s2;
+  NB_CUDA(cudaStreamWaitEvent(s2, mg.ev_fork, 0));
   for (int l = Lm - 1; l >= 2; --l) {
-    NB_TRY(mg_rstr<T>(mg, V::r(mg.lv[l]), V::r(mg.lv[l + 1]), l, true, s));
-    NB_TRY(mg_schwarz<T>(mg, V::e(mg.lv[l]), V::r(mg.lv[l]), l, s));
+    NB_TRY(mg_rstr<T>(mg, V::r(mg.lv[l]), V::r(mg.lv[l + 1]), l, true, s2));
+    NB_TRY(mg_schwarz<T>(mg, V::e(mg.lv[l]), V::r(mg.lv[l]), l, V::A2(mg), V::B2(mg), true,
+                         s2));
   }
   MgLevel &C = mg.lv[1];
-  NB_TRY(mg_rstr<T>(mg, V::r(C), V::r(mg.lv[2]), 1, false, s));
+  NB_TRY(mg_rstr<T>(mg, V::r(C), V::r(mg.lv[2]), 1, false, s2));
   if (std::is_same<T, double>::value) {
-    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
-    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));  // hsmg_coarse_solve
-    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
-    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s));
-    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
+    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s2));
+    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s2));  // hsmg_coarse_solve
+    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s2));
+    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s2));
+    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s2));
   } else {
     // FP64 coarse solve between the FP32 legs
-    k_to_f64<<<grid_for(C.n), 256, 0, s>>>(C.r, C.r_f, C.n);
-    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s));
-    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s));
-    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s));
-    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s));
-    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s));
-    k_to_f32<<<grid_for(C.n), 256, 0, s>>>(C.e_f, C.e, C.n);
+    k_to_f64<<<grid_for(C.n), 256, 0, s2>>>(C.r, C.r_f, C.n);
+    NB_TRY(vec_mask<double>(C.r, C.mask, C.nmask, s2));
+    NB_TRY(vec_copy<double>(C.e, C.r, C.n, s2));
+    NB_TRY(gs_exec(C.gs, C.e, 1, 1, 0, s2));
+    if (mg.coarse_exact) NB_TRY(coarse_apply(mg, s2));
+    NB_TRY(vec_mask<double>(C.e, C.mask, C.nmask, s2));
+    k_to_f32<<<grid_for(C.n), 256, 0, s2>>>(C.e_f, C.e, C.n);
     NB_CUDA(cudaGetLastError());
   }
   for (int l = 2; l <= Lm - 1; ++l)
-    NB_TRY(mg_intp_add<T>(mg, V::e(mg.lv[l]), V::e(mg.lv[l - 1]), l - 1, true, s));
+    NB_TRY(mg_intp_add<T>(mg, V::e(mg.lv[l]), V::e(mg.lv[l - 1]), l - 1, true, s2));
+  NB_CUDA(cudaEventRecord(mg.ev_join, s2));
+  NB_CUDA(cudaStreamWaitEvent(s, mg.ev_join, 0));
   return mg_intp_add<T>(mg, zT, V::e(mg.lv[Lm - 1]), Lm - 1, true, s);
 }
 
@@ -1516,6 +1561,11 @@ int mg_setup_coarse(Multigrid *mg, const double *g, cudaStream_t s) {
   mg->coarse_exact = true;
   NB_CUDA(cudaStreamSynchronize(s));
   return NB_OK;
+}
+
+int mg_solve_f32(Multigrid &mg, cudaStream_t s) {
+  if (mg.precision != 32) return fail(NB_ERR_STATE, "mg_solve_f32: FP32 smoother only");
+  return vcycle<float>(mg, mg.z_f, mg.lv[mg.nlev].r_f, s);
 }
 
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s) {

@@ -34,6 +34,13 @@ struct Multigrid {
   double *w = nullptr;            // interpolation result
   int precision = 64;             // 64, or 32: FP32 Schwarz smoother and transfers
   float *A_f = nullptr, *B_f = nullptr, *z_f = nullptr;
+  // the levels below the finest run on a second stream beside the finest
+  // level's smoother (the cycle is additive): their own extended work
+  // arrays, the stream and the fork / join events
+  double *A2 = nullptr, *B2 = nullptr;
+  float *A2_f = nullptr, *B2_f = nullptr;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // exact coarse solve (replacing the reference's copy + dssum): the
   // Galerkin operator R A P of the V-cycle's own transfer chain on the
   // unmasked vertices, probed with 27 colours, inverted densely
@@ -63,5 +70,8 @@ int mg_setup_coarse(Multigrid *mg, const double *g, cudaStream_t s);
 void mg_set_fixed_kernels(bool on);
 // h1mg_solve (hsmg.f:960-1034): z = M^-1 rhs; masks rhs in place.
 int mg_solve(Multigrid &mg, double *z, double *rhs, cudaStream_t s);
+// The FP32 cycle alone (precision 32): from the finest level's r_f, which
+// the caller filled with float(rhs) of a masked rhs, to z_f.
+int mg_solve_f32(Multigrid &mg, cudaStream_t s);
 
 }  // namespace nb

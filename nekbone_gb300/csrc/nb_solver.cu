@@ -434,10 +434,11 @@ int vec_convert(T *a, const S *b, long n, cudaStream_t s) {
 }
 template <typename T>
 int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
-              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s) {
+              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s,
+              const float *mf, T *mout) {
   const int gr = std::min(grid_for(n), wk.grid_up);
   k_glsc3<T><<<gr, 256, 0, s>>>(a, b, m, n, wk.partial_dot, wk.counters + 2, out,
-                                sc, mode, wk.hist, iter);
+                                sc, mode, wk.hist, iter, mf, mout);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }
@@ -452,8 +453,8 @@ template int vec_copy<double>(double *, const double *, long, cudaStream_t);
 template int vec_copy<float>(float *, const float *, long, cudaStream_t);
 template int vec_convert<float, double>(float *, const double *, long, cudaStream_t);
 template int vec_convert<double, float>(double *, const float *, long, cudaStream_t);
-template int vec_glsc3<double>(const double *, const double *, const double *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t);
-template int vec_glsc3<float>(const float *, const float *, const float *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t);
+template int vec_glsc3<double>(const double *, const double *, const double *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t, const float *, double *);
+template int vec_glsc3<float>(const float *, const float *, const float *, long, CgWork &, double *, CgScalars *, int, int, cudaStream_t, const float *, float *);
 
 // ------------------------------------------------------------ ax launch --
 // launch_ax<T> is instantiated in nb_ax_f64.cu / nb_ax_f32.cu (one
@@ -503,6 +504,7 @@ static int cg_begin_t(Operator &op, CgWork &wk, T *x, const T *f, const T *c,
                       T *r, bool zero_x, int niter, cudaStream_t s) {
   const long n = op.n;
   NB_TRY(wk.ensure(op, niter));
+  wk.r32_ready = false;
   if (zero_x) NB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));  // rzero(x)
   NB_TRY(vec_copy<T>(r, f, n, s));                                 // copy(r,f)
   NB_TRY(maskit_dev<T>(op, r, s));
@@ -522,9 +524,17 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
     if (M) {
       if (!std::is_same<T, double>::value)
         return fail(NB_ERR_UNSUPPORTED, "preconditioned CG is FP64 only");
-      NB_TRY(M->apply((double *)z, (double *)r, s));
       zz = z;
-      NB_TRY(vec_glsc3<T>(r, c, z, n, wk, wk.dot_out + 1, wk.sc, 2, iter, s));
+      if (wk.r32_ready && M->r32_in()) {
+        // the update already wrote float(r); z arrives in FP32 and becomes
+        // FP64 inside glsc3(r, c, z) (same values as the conversion passes)
+        NB_TRY(M->apply_f32(s));
+        NB_TRY(vec_glsc3<T>(r, c, z, n, wk, wk.dot_out + 1, wk.sc, 2, iter, s,
+                            M->z32_out(), z));
+      } else {
+        NB_TRY(M->apply((double *)z, (double *)r, s));
+        NB_TRY(vec_glsc3<T>(r, c, z, n, wk, wk.dot_out + 1, wk.sc, 2, iter, s));
+      }
     } else if (z && z != r && iter == niter) {
       // hsmg_dum's solveM leaves z = r of the last iteration (hsmg_dum.f:9-14)
       NB_TRY(vec_copy<T>(z, r, n, s));
@@ -556,10 +566,12 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
       k_set_alpha<<<1, 1, 0, s>>>(wk.sc, wk.dot_out + 2);
       NB_CUDA(cudaGetLastError());
     }
+    float *r32 = M ? M->r32_in() : nullptr;
     k_cg_update<T><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, n, wk.partial_up,
                                               wk.counters + 1, wk.sc,
                                               iter < wk.hist_len ? wk.hist : nullptr,
-                                              iter, M == nullptr);
+                                              iter, M == nullptr, r32);
+    wk.r32_ready = r32 != nullptr;
     NB_CUDA(cudaGetLastError());
   }
   return NB_OK;

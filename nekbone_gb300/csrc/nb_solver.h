@@ -66,6 +66,8 @@ struct CgWork {
   // the FP32 metric of the solve in progress has one block for all
   // elements (set by the mixed solver around its inner CG)
   int g32_uniform = 0;
+  // the preconditioner's FP32 input holds float(r) of the current r
+  bool r32_ready = false;
   ~CgWork();
   int ensure(const Operator &op, int niter);
   int ensure_scratch(size_t bytes);
@@ -121,7 +123,8 @@ template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s);
 template <typename T>
 int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
-              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s);
+              double *out, CgScalars *sc, int mode, int iter, cudaStream_t s,
+              const float *mf = nullptr, T *mout = nullptr);
 template <typename T>
 int vec_add2s1(T *a, const T *b, const double *c1_dev, double c1, long n,
                cudaStream_t s);
@@ -142,6 +145,13 @@ int apply_ax(const Operator &op, T *w, const T *u, const T *g, cudaStream_t s);
 // precond: nullptr for the identity (hsmg_dum.f), else z = M^-1 r.
 struct Precond {
   virtual int apply(double *z, double *r, cudaStream_t s) = 0;
+  // An FP32 preconditioner on an r that is already masked may take its
+  // input as float(r) written by the CG update (r32_in, null when it cannot)
+  // and leave its result in FP32 (z32_out) for the r.z product to convert:
+  // apply_f32 runs it from that input.
+  virtual float *r32_in() { return nullptr; }
+  virtual int apply_f32(cudaStream_t) { return 1; }
+  virtual const float *z32_out() { return nullptr; }
   virtual ~Precond() {}
 };
 int cg_device(Operator &op, CgWork &wk, double *x, const double *f,
