@@ -332,6 +332,10 @@ int nb_batch_set_tuning(nb_batch *batch, int lx1, int epb32, int rd32, int epb64
  * inner_iters FP32 CG iterations, at most max_outer cycles) as one graph
  * launch on the library stream; x starts at 0. */
 int nb_batch_solve(nb_batch *batch, double tol, int inner_iters, int max_outer);
+/* Inner stopping of later solves: 0 (default) every cycle runs inner_iters
+ * FP32 iterations; itol in (0, 1) ends each problem's inner CG once its
+ * r'Cr fell by itol^2 (its residual by itol), at most inner_iters. */
+int nb_batch_set_inner_tol(nb_batch *batch, double itol);
 /* per problem: cycles, inner iterations, final |r|_C / |f|_C (synchronises) */
 int nb_batch_result(const nb_batch *batch, int prob, int *outer, int *inner, double *relres);
 /* cycles the last solve's loop ran */

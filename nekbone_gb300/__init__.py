@@ -52,7 +52,7 @@ EXPORTS = (
     "nb_time_cg_kernels", "nb_glsc3_noalloc", "nb_time_cg_kernels_f32",
     "nb_batch_create", "nb_batch_destroy", "nb_batch_info", "nb_batch_problem",
     "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
-    "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_result", "nb_batch_cycles",
+    "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_set_inner_tol", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse",
@@ -112,6 +112,7 @@ for _name, _args in (
         ("nb_batch_get_tuning", [_p, _i, _p, _p, _p, _p, _p]),
         ("nb_batch_set_tuning", [_p, _i, _i, _i, _i]),
         ("nb_batch_solve", [_p, _d, _i, _i]),
+        ("nb_batch_set_inner_tol", [_p, _d]),
         ("nb_batch_result", [_p, _i, _p, _p, _p]),
         ("nb_batch_cycles", [_p, _p]),
         ("nb_batch_rhs_in", [_p, _p]),
@@ -579,6 +580,11 @@ class Batch:
 
     def set_tuning(self, lx: int, epb32: int, rd32: int, epb64: int) -> None:
         _check(lib.nb_batch_set_tuning(self._h, lx, epb32, rd32, epb64))
+
+    def set_inner_tol(self, itol: float) -> None:
+        """0: fixed inner_iters per cycle; > 0: each problem's inner CG stops
+        once its residual fell by itol (at most inner_iters)"""
+        _check(lib.nb_batch_set_inner_tol(self._h, _C.c_double(itol)))
 
     def solve(self, tol: float = 1e-10, inner_iters: int = 20, max_outer: int = 50) -> None:
         """enqueue the whole solve (one graph launch) on the library stream"""

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ double red[32];
   const int ch = blockIdx.x;
   const int prob = gch_prob[ch];
-  if (!sc[prob].active) return;
+  if (!sc[prob].active || !sc[prob].iactive) return;
   const int g = gch_g0[ch] + threadIdx.x;
   float part = 0.f;
   if (g < gch_g0[ch + 1]) {
@@ -109,8 +109,7 @@ __global__ void __launch_bounds__(kThreads)
               const int *__restrict__ off, const unsigned *__restrict__ idx,
               const int *__restrict__ gch_g0, const int *__restrict__ gch_prob,
               const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_gs,
-              const double *__restrict__ part_ax, unsigned *cnt, double tol, int inner_iters,
-              int max_outer) {
+              const double *__restrict__ part_ax, unsigned *cnt, double tol, int max_outer) {
   __shared__ double red[32];
   const int ch = blockIdx.x;
   const int prob = gch_prob[ch];
@@ -154,7 +153,6 @@ __global__ void __launch_bounds__(kThreads)
       S.rtr = s1 + s2;
       S.rn = sqrt(s1 + s2);
       S.outer += 1;
-      S.inner += inner_iters;
       const bool converged = S.rn <= tol * S.rn0;
       S.active = (!converged && S.outer < max_outer) ? 1 : 0;
     }
@@ -162,17 +160,20 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Inner FP32 update (k_cg_update per problem): x += alpha p, r -= alpha w,
-// r'Cr; the problem's last chunk forms rtz1 and beta (z = r).
+// r'Cr; the problem's last chunk forms rtz1 and beta (z = r), counts the
+// iteration and, with itol > 0, ends the problem's inner CG of this cycle
+// once r'Cr <= itol^2 of the cycle's first (it: the iteration within the
+// cycle, at most max_inner).
 __global__ void __launch_bounds__(kThreads)
     k_bupd(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
            const float *__restrict__ w, const float *__restrict__ c,
            const long *__restrict__ pch_q0, const int *__restrict__ pch_prob,
            const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_pt,
-           unsigned *cnt) {
+           unsigned *cnt, int it, int max_inner, double itol) {
   __shared__ double red[32];
   const int ch = blockIdx.x;
   const int prob = pch_prob[ch];
-  if (!sc[prob].active) return;
+  if (!sc[prob].active || !sc[prob].iactive) return;
   const float alpha = float(sc[prob].alpha);
   const float alphm = -alpha;
   const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
@@ -196,6 +197,8 @@ __global__ void __launch_bounds__(kThreads)
       S.rtz2 = S.rtz1;
       S.rtz1 = rtr;
       S.beta = S.rtz2 != 0.0 ? S.rtz1 / S.rtz2 : 0.0;
+      S.inner += 1;
+      if (it >= max_inner || (itol > 0.0 && rtr <= itol * itol * S.irtr0)) S.iactive = 0;
     }
   }
 }
@@ -228,7 +231,9 @@ __global__ void __launch_bounds__(kThreads)
     const double rtz = block_sum_array(part_pt + P.pc0, P.npc, red);
     if (threadIdx.x == 0) {
       sc[prob].rtz1 = rtz;
+      sc[prob].irtr0 = rtz;
       sc[prob].beta = 0.0;
+      sc[prob].iactive = 1;
     }
   }
 }
@@ -263,6 +268,7 @@ __global__ void __launch_bounds__(kThreads)
       S.rtr = ff;
       S.outer = 0;
       S.inner = 0;
+      S.iactive = 0;
       S.active = (S.rn0 > 0.0 && max_outer > 0) ? 1 : 0;
     }
   }
@@ -358,6 +364,7 @@ __global__ void k_set_active(BatchScalars *sc, int nprob) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < nprob) {
     sc[p].active = 1;
+    sc[p].iactive = 1;
     sc[p].rn = 1.0;
     sc[p].beta = 0.0;
   }
@@ -460,8 +467,9 @@ struct Batch {
   cudaStream_t cap = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  double g_tol = -1.0;
+  double g_tol = -1.0, g_itol = -1.0;
   int g_inner = -1, g_outer = -1;
+  double itol = 0.0;  // 0: every cycle runs inner iterations; > 0: per-problem stop
 
   ~Batch() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -545,26 +553,27 @@ struct Batch {
   }
 
   // one inner FP32 iteration / the FP64 defect, for all active problems
-  int inner_iteration(int it, cudaStream_t s) const {
+  int inner_iteration(int it, int max_inner, cudaStream_t s) const {
     NB_TRY(launch_inner_ax(it, s));
     k_bgs_fin<<<ngc, kThreads, 0, s>>>(w32, p32, c32, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
                                        part_ax, cnt);
     NB_CUDA(cudaGetLastError());
     k_bupd<<<npc, kThreads, 0, s>>>(e32, r32, p32, w32, c32, pch_q0, pch_prob, pb, sc, part_pt,
-                                     cnt + nprob);
+                                     cnt + nprob, it, max_inner, itol);
     NB_CUDA(cudaGetLastError());
     return NB_OK;
   }
-  int defect(double tol, int inner, int max_outer, cudaStream_t s) const {
+  int defect(double tol, int max_outer, cudaStream_t s) const {
     NB_TRY(launch_defect_ax(s));
     k_bgs_res<<<ngc, kThreads, 0, s>>>(w, x, f, r, c, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
-                                       part_ax, cnt + 2 * nprob, tol, inner, max_outer);
+                                       part_ax, cnt + 2 * nprob, tol, max_outer);
     NB_CUDA(cudaGetLastError());
     return NB_OK;
   }
 
   int build_graph(double tol, int inner, int max_outer) {
-    if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer) return NB_OK;
+    if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer && itol == g_itol)
+      return NB_OK;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
@@ -614,8 +623,8 @@ struct Batch {
     k_bscale<<<npc, kThreads, 0, cap>>>(r32, e32, r, c32, pch_q0, pch_prob, pb, sc, part_pt,
                                         cnt + 3 * nprob);
     if (cudaGetLastError() != cudaSuccess) st = fail(NB_ERR_CUDA, "batched solve: capture");
-    for (int it = 1; it <= inner && !st; ++it) st = inner_iteration(it, cap);
-    if (!st) st = defect(tol, inner, max_outer, cap);
+    for (int it = 1; it <= inner && !st; ++it) st = inner_iteration(it, inner, cap);
+    if (!st) st = defect(tol, max_outer, cap);
     if (!st) {
       k_bcontrol<<<1, kThreads, 0, cap>>>(sc, nprob, cycles, 0, max_cycles, h);
       if (cudaGetLastError() != cudaSuccess) st = fail(NB_ERR_CUDA, "batched solve: capture");
@@ -629,6 +638,7 @@ struct Batch {
     g_tol = tol;
     g_inner = inner;
     g_outer = max_outer;
+    g_itol = itol;
     return NB_OK;
   }
 };
@@ -1071,6 +1081,14 @@ int nb_batch_tune(nb_batch *b, int reps) {
 }
 
 // Enqueues the whole solve (one graph launch) on the library stream.
+int nb_batch_set_inner_tol(nb_batch *b, double itol) {
+  clear_status();
+  if (!b) return fail(NB_ERR_HANDLE, "null batch");
+  if (!(itol >= 0.0 && itol < 1.0)) return fail(NB_ERR_ARG, "inner tolerance %g", itol);
+  b->B.itol = itol;
+  return NB_OK;
+}
+
 int nb_batch_solve(nb_batch *b, double tol, int inner_iters, int max_outer) {
   clear_status();
   if (!b) return fail(NB_ERR_HANDLE, "null batch");

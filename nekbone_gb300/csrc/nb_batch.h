@@ -20,9 +20,10 @@ namespace nb {
 struct BatchScalars {
   double rtz1, rtz2, beta, pap, alpha, rtr;  // inner CG
   double rn0, rn;                            // |f|_C and current |r|_C (FP64)
+  double irtr0;                              // the cycle's first inner r'Cr
   int active;                                // 1 while |r|/|f| > tol
   int outer, inner;                          // cycles and inner iterations
-  int pad;
+  int iactive;                               // 1 while the cycle's inner CG runs
 };
 
 // Per-problem index ranges into the concatenated batch arrays.

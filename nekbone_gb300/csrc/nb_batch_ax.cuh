@@ -43,7 +43,8 @@ __global__ void __launch_bounds__(LX * LX * EPB)
   const bool in_range = el < a.nel;
   const int e = a.el0 + (in_range ? el : 0);
   const int prob = a.el_prob[e];
-  const bool act = in_range && a.sc[prob].active;
+  // the inner operator (MODE 1) skips problems whose inner CG ended
+  const bool act = in_range && a.sc[prob].active && (MODE != 1 || a.sc[prob].iactive);
   if (!__syncthreads_or(act)) return;  // every element of the CTA converged
   const size_t base = size_t(a.pt0) + size_t(in_range ? el : 0) * L3;
   auto &E = sm.el[z];
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(LX * LX)
   const int i = threadIdx.x, j = threadIdx.y;
   const int e = a.el0 + blockIdx.x;
   const int prob = a.el_prob[e];
-  if (!a.sc[prob].active) return;   // the whole CTA: one element
+  if (!a.sc[prob].active || (MODE == 1 && !a.sc[prob].iactive)) return;  // one element
   const size_t base = size_t(a.pt0) + size_t(blockIdx.x) * L3;
   if (TMAG && t == 0) {
     constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));

@@ -213,3 +213,37 @@ def test_even_odd_forms_agree(torch):
             assert b.result(p)[2] <= 1e-10
     assert np.max(np.abs(xs[0] - xs[1])) <= 1e-8 * np.max(np.abs(xs[0]))
     b.close()
+
+
+def test_inner_tolerance_stops_each_problem(torch):
+    """With an inner tolerance each problem's FP32 CG ends its cycle once its
+    residual fell by itol (at most inner_iters): every problem still meets
+    the outer tolerance by the oracle's residual, and the small problems
+    stop early."""
+    import nekbone_gb300 as nb
+    b = nb.Batch(BOXES)
+    b.setup(17)
+    b.tune(1)
+    b.set_inner_tol(1e-4)
+    b.solve(1e-10, 60, 40)
+    nb.sync()
+    early = 0
+    for p, (nx, ny, nz, lx) in enumerate(BOXES):
+        outer, inner, rr = b.result(p)
+        assert rr <= 1e-10, (p, rr)
+        assert 1 <= outer and outer <= inner <= 60 * outer
+        early += inner < 60 * outer
+        a = _problem_arrays(torch, b, p)
+        ctx = O.Ctx(nx, ny, nz, lx, mask_mode=1)
+        r = a["f"] - ctx.ax(a["x"], a["g"])
+        rel = np.sqrt(np.sum(r * a["c"] * r)) / np.sqrt(np.sum(a["f"] * a["c"] * a["f"]))
+        assert rel <= 2e-10, (p, rel)
+    assert early >= 1
+    # back to the fixed count: every cycle runs inner_iters again
+    b.set_inner_tol(0.0)
+    b.solve(1e-10, 20, 40)
+    nb.sync()
+    for p in range(len(BOXES)):
+        outer, inner, rr = b.result(p)
+        assert inner == 20 * outer and rr <= 1e-10
+    b.close()
