@@ -143,3 +143,26 @@ def test_fixed_size_kernels_bitwise(torch, precision, levels):
         nb.set_mg_fixed_kernels(True)
     assert np.abs(out[True]).max() > 0
     assert np.array_equal(out[True], out[False])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_two_stream_vcycle_repeatable(torch, precision):
+    """The levels below the finest run on a second stream beside the finest
+    smoother: repeated V-cycles on the same right-hand side are bitwise
+    equal (no ordering left to chance), with and without the exact coarse
+    solve."""
+    m, g, c, f = _setup(torch, 6, 12, deformed=True)
+    for levels, exact in (([2, 5, 11], False), ([1, 3, 7, 11], True)):
+        m.mg_setup(levels, precision=precision)
+        if exact:
+            m.mg_setup_coarse(g.data_ptr())
+        outs = []
+        for _ in range(4):
+            z = torch.zeros_like(f)
+            rhs = f.clone()
+            m.mg_solve(z.data_ptr(), rhs.data_ptr())
+            torch.cuda.synchronize()
+            outs.append(z.cpu().numpy())
+        assert np.abs(outs[0]).max() > 0
+        for o in outs[1:]:
+            assert np.array_equal(outs[0], o)
