@@ -137,6 +137,10 @@ void semhat_(double *a, double *b, double *c, double *d, double *z,
 void set_vert_box_(int64_t *glo_num, const int *nx);
 /* cubic (driver.f:196-247) */
 void cubic_(int *mx, int *my, int *mz, const int *np);
+/* get_exyz (prox_dssum.f:75-86): brick position (1-based) of global
+ * element eg in a nelx x nely x nelz box. */
+void get_exyz_(int *ex, int *ey, int *ez, const int *eg, const int *nelx, const int *nely,
+               const int *nelz);
 /* setup_g (prox_setup.f:27-52) on the published mesh */
 void setup_g_(double *g);
 /* set_multiplicity (driver.f:274-291) on the published gsh */

@@ -45,7 +45,7 @@ EXPORTS = (
     "gs_free_", "dssum_", "glsc3_", "add2s1_", "add2s2_", "mxm_", "cg_", "ax_",
     "ax_e_", "local_grad3_", "local_grad3_t_", "maskit_", "solvem_",
     "h1mg_setup_", "h1mg_solve_", "zwgll_", "semhat_", "set_vert_box_",
-    "cubic_", "setup_g_", "set_multiplicity_", "set_f_", "nb_mesh_create",
+    "cubic_", "get_exyz_", "setup_g_", "set_multiplicity_", "set_f_", "nb_mesh_create",
     "nb_mesh_destroy", "nb_mesh_npts", "nb_mesh_info", "nb_setup_g",
     "nb_set_multiplicity", "nb_rhs_uniform", "nb_ax", "nb_dssum", "nb_cg",
     "nb_cg_f32", "nb_cg_mixed", "nb_cg_tol", "nb_sync", "nb_stream",
@@ -193,6 +193,15 @@ def cubic(np_: int):
     mx, my, mz = _C.c_int(), _C.c_int(), _C.c_int()
     lib.cubic_(_C.byref(mx), _C.byref(my), _C.byref(mz), _ref(np_))
     return mx.value, my.value, mz.value
+
+
+def get_exyz(eg: int, nelx: int, nely: int, nelz: int):
+    """Brick position (ex, ey, ez), 1-based, of global element eg
+    (prox_dssum.f get_exyz)."""
+    ex, ey, ez = _C.c_int(), _C.c_int(), _C.c_int()
+    lib.get_exyz_(_C.byref(ex), _C.byref(ey), _C.byref(ez), _ref(eg), _ref(nelx),
+                  _ref(nely), _ref(nelz))
+    return ex.value, ey.value, ez.value
 
 
 # ----------------------------------------------------------- gather-scatter --

@@ -721,6 +721,12 @@ void semhat_(double *a, double *b, double *c, double *d, double *z, double *w,
 
 void cubic_(int *mx, int *my, int *mz, const int *np) { cubic(mx, my, mz, *np); }
 
+void get_exyz_(int *ex, int *ey, int *ez, const int *eg, const int *nelx, const int *nely,
+               const int *nelz) {
+  (void)nelz;  // the reference takes it and does not use it
+  get_exyz(ex, ey, ez, *eg, *nelx, *nely);
+}
+
 void set_vert_box_(int64_t *glo_num, const int *nx) {
   clear_status();
   State &S = st();

@@ -89,3 +89,19 @@ def test_batch_rejects_bad_problems_without_a_gpu():
         nb.Batch([(0, 2, 2, 6)])
     with pytest.raises(nb.NekboneError):
         nb.Batch([])
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 4), (3, 2, 5), (1, 1, 7), (6, 1, 1)])
+def test_get_exyz_brick_positions(dims):
+    """get_exyz (prox_dssum.f:75-86): element eg of the brick order sits at
+    (ex, ey, ez) with eg = ex + nelx*(ey-1) + nelx*nely*(ez-1); every
+    position once."""
+    import nekbone_gb300 as nb
+    nelx, nely, nelz = dims
+    seen = set()
+    for eg in range(1, nelx * nely * nelz + 1):
+        ex, ey, ez = nb.get_exyz(eg, nelx, nely, nelz)
+        assert 1 <= ex <= nelx and 1 <= ey <= nely and 1 <= ez <= nelz
+        assert ex + nelx * (ey - 1) + nelx * nely * (ez - 1) == eg
+        seen.add((ex, ey, ez))
+    assert len(seen) == nelx * nely * nelz
