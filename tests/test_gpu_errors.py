@@ -1,0 +1,79 @@
+"""Error paths of the device API: every rejected call fails with a status
+(NekboneError) before it touches device memory, and the library stays
+usable afterwards."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nb():
+    import nekbone_gb300 as m
+    return m
+
+
+def test_mesh_size_and_argument_limits(nb):
+    with pytest.raises(nb.NekboneError):
+        nb.DeviceMesh(128, 128, 128, 16, mask_mode=1)   # 8.6e9 points > 2^31-1
+    with pytest.raises(nb.NekboneError):
+        nb.DeviceMesh(0, 2, 2, 6, mask_mode=1)
+    with pytest.raises(nb.NekboneError):
+        nb.DeviceMesh(2, 2, 2, 6, mask_mode=2)
+    m = nb.DeviceMesh(2, 2, 2, 6, mask_mode=1)       # still usable
+    assert m.n == 8 * 216
+    m.close()
+
+
+def test_multigrid_argument_checks(nb):
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(3, 3, 3, 8, mask_mode=1)
+    with pytest.raises(nb.NekboneError):
+        m.mg_setup([2, 4, 6], precision=64)            # finest order must be lx1-1
+    with pytest.raises(nb.NekboneError):
+        m.mg_setup([2, 4, 7], precision=16)            # 64 or 32
+    with pytest.raises(nb.NekboneError):
+        m.mg_setup([7], precision=64)                  # at least two levels
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device="cuda")
+    m.setup_g(g.data_ptr())
+    m.mg_setup([2, 4, 7], precision=64)
+    with pytest.raises(nb.NekboneError):
+        m.mg_setup_coarse(g.data_ptr())                # coarsest level not order 1
+    m.close()
+
+
+def test_exact_coarse_size_limit(nb):
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(32, 32, 32, 3, mask_mode=1)     # 31^3 coarse vertices
+    g = torch.empty(6 * m.n, dtype=torch.float64, device="cuda")
+    m.setup_g(g.data_ptr())
+    m.mg_setup([1, 2], precision=64)
+    with pytest.raises(nb.NekboneError):
+        m.mg_setup_coarse(g.data_ptr())
+    m.close()
+
+
+def test_pcg_needs_multigrid_and_batch_checks(nb):
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(2, 2, 2, 6, mask_mode=1)
+    n = m.n
+    v = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(4)]
+    g = torch.zeros(6 * n, dtype=torch.float64, device="cuda")
+    with pytest.raises(nb.NekboneError):
+        m.pcg_tol(v[0].data_ptr(), v[1].data_ptr(), g.data_ptr(), v[2].data_ptr(), 1e-10)
+    m.close()
+    b = nb.Batch([(2, 2, 2, 6), (1, 1, 2, 8)])
+    with pytest.raises(nb.NekboneError):
+        b.solve(1e-10, 20, 5)                          # before setup
+    b.setup(3)
+    with pytest.raises(nb.NekboneError):
+        b.set_inner_tol(1.5)
+    with pytest.raises(nb.NekboneError):
+        b.solve(1e-10, 0, 5)
+    b.solve(1e-10, 20, 20)                             # still usable
+    nb.sync()
+    assert all(b.result(p)[2] <= 1e-10 for p in range(b.nprob))
+    b.close()
