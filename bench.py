@@ -442,6 +442,7 @@ def run_ours(a, rank, world, local):
     nb.sync()
     torch.cuda.synchronize()
     ms, value = replica_rate(e0.elapsed_time(e1), n, niter, a.steps, world, dev)
+    unique = ((lx - 1) * nel + 1) ** 3
     clocks = clk.summary()
     ms_per_step = ms / a.steps
     launches_per_step = 2 + 3 * niter  # copy/mask/glsc3 + 3 kernels per iteration
@@ -491,7 +492,9 @@ def run_ours(a, rank, world, local):
            "config": {"workload": f"cg, {nel}^3 elements, lx1={lx}, {niter} FP64 iterations per step",
                       "n": n, "mask": "full Dirichlet", "rhs": "seeded uniform[-1,1] per global DOF",
                       "l2": "inputs larger than L2 (453 MB per vector)", "setup_s": setup_s,
-                      "setup_host_topology_s": setup_host_s},
+                      "setup_host_topology_s": setup_host_s,
+                      # unique global DOFs of the box, (N nelx + 1)(N nely + 1)(N nelz + 1)
+                      "unique_dofs": unique, "value_unique_gdof_iter_per_s": value * unique / n},
            "gpu_launches": launches_per_step * a.steps, "clocks": clocks, "roofline": roofline}
 
     # ---- mixed vs FP64 time to tolerance
