@@ -43,10 +43,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "GDOF·iter/s (lx1=12, 32^3 elems); mixed vs FP64 GPU time to rel. resid 1e-10"
 # FP64 FMA throughput of one GB300 (an FMA-chain probe: 1/72 of FP32)
 FP64_PEAK_TFLOPS = 1.055
-# DRAM read + write bytes per point of k_ax_eo<12,1> (ncu, 16^3 elements:
-# 500.3 MB + 98.4 MB over 7,077,888 points); the kernel streams, so traffic
-# scales with n
-DRAM_BYTES_PER_POINT_AX_EO = (500.333824e6 + 98.385920e6) / 7077888
+# DRAM read + write bytes per point of k_ax_eo4<double,12,1> (ncu, 16^3
+# elements: 531.7 MB + 120.9 MB over 7,077,888 points); the kernel streams,
+# so traffic scales with n
+DRAM_BYTES_PER_POINT_AX_EO = (531.699456e6 + 120.930048e6) / 7077888
 UNIT = "GDOF*iter/s"
 
 
@@ -459,9 +459,11 @@ def run_ours(a, rank, world, local):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak,
                 # DRAM bytes per launch: ncu capture of the same kernel on 16^3
-                # elements (84.6 B per point read + written), scaled by n
+                # elements (92.2 B per point read + written), scaled by n
                 "traffic": DRAM_BYTES_PER_POINT_AX_EO * n if (eo and lx == 12) else None,
-                "kernel": f"k_ax_eo<{lx},1> (fused element operator, even-odd contractions)"
+                "kernel": (f"k_ax_eo4<double,{lx},1> (fused element operator, even-odd "
+                           f"contractions, four CTAs per SM)") if (eo and lx == 12) else
+                          f"k_ax_eo<double,{lx},1> (fused element operator, even-odd contractions)"
                           if eo else f"k_ax_impl<double,{lx},1,false> (fused element operator)",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
                 "kernel_ms": {"ax": kms[0], "gs_fin": kms[1], "update": kms[2]},
@@ -469,7 +471,7 @@ def run_ours(a, rank, world, local):
                 "fp64_pipe": {"reference_flops_per_point": flops_pt,
                               "tflops_reference_count": flops_pt * n / (kms[0] * 1e-3) / 1e12,
                               "peak_tflops": FP64_PEAK_TFLOPS,
-                              "ncu_pipe_active": 0.904 if (eo and lx == 12) else None}}
+                              "ncu_pipe_active": 0.919 if (eo and lx == 12) else None}}
 
     # the FP32 iteration of the mixed solver's inner CG, same mesh
     f32, g32, c32 = f.float(), g.float(), c.float()

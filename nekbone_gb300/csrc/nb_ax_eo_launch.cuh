@@ -9,13 +9,19 @@ namespace nb {
 template <typename T, int LX, int MODE, bool TMAG>
 int launch_ax_eo_shape(AxArgs<T> a, const T *eo, cudaStream_t s) {
   const size_t sm = ax_eo_smem_bytes<T, LX, TMAG>();
+  // FP64 at lx1 = 12 (CG and apply): the four-CTA form, 96 registers with
+  // a few bytes spilled, keeps four CTAs per SM instead of two at 134
+  // registers (FP64 pipe 92 % busy instead of 86 %); the other shapes spill
+  // too much under that cap
+  void (*fn)(AxArgs<T>, const T *);
+  if constexpr (sizeof(T) == 8 && LX == 12 && MODE != 2) fn = k_ax_eo4<T, LX, MODE, TMAG>;
+  else fn = k_ax_eo<T, LX, MODE, TMAG>;
   static bool attr_set = false;
   if (!attr_set) {
-    NB_CUDA(cudaFuncSetAttribute(k_ax_eo<T, LX, MODE, TMAG>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
+    NB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(sm)));
     attr_set = true;
   }
-  k_ax_eo<T, LX, MODE, TMAG><<<a.nelt, dim3(LX, LX), sm, s>>>(a, eo);
+  fn<<<a.nelt, dim3(LX, LX), sm, s>>>(a, eo);
   NB_CUDA(cudaGetLastError());
   return NB_OK;
 }

@@ -795,8 +795,24 @@ __device__ __forceinline__ void eo_line(const T *v, const T *Ec, const T *Oc, T 
 }
 
 template <typename T, int LX, int MODE, bool TMAG>
+__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const T *eo);
+
+template <typename T, int LX, int MODE, bool TMAG>
 __global__ void __launch_bounds__(LX * LX)
     k_ax_eo(AxArgs<T> a, const T *eo) {
+  ax_eo_body<T, LX, MODE, TMAG>(a, eo);
+}
+// The same with four CTAs per SM asked for (the FP64 lx1 = 12 operator):
+// the FP64 pipe is its bound, and a fourth CTA's warps cover the barrier
+// and shared-memory waits
+template <typename T, int LX, int MODE, bool TMAG>
+__global__ void __launch_bounds__(LX * LX, 4)
+    k_ax_eo4(AxArgs<T> a, const T *eo) {
+  ax_eo_body<T, LX, MODE, TMAG>(a, eo);
+}
+
+template <typename T, int LX, int MODE, bool TMAG>
+__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const T *eo) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   AxEoShared<T, LX, TMAG> &sm = *reinterpret_cast<AxEoShared<T, LX, TMAG> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
