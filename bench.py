@@ -544,13 +544,19 @@ def run_ours(a, rank, world, local):
         wn = tuple(t.numpy() for t in work)
         hb.cg(fn, gn, cn, niter, 0.0, wn)      # warm-up
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(a.steps):
-            hb.cg(fn, gn, cn, niter, 0.0, wn)
-        e2e_s = (time.perf_counter() - t0) / a.steps
+        calls = []
+        with Clocks(local) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(a.steps):
+                t1 = time.perf_counter()
+                hb.cg(fn, gn, cn, niter, 0.0, wn)
+                calls.append((time.perf_counter() - t1) * 1e3)
+            e2e_s = (time.perf_counter() - t0) / a.steps
         out["e2e"] = {"value": world * n * niter / e2e_s / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": 64 * n, "d2h_bytes_per_step": 40 * n,
-                      "ms_per_step": e2e_s * 1e3, "call": "cg_ (C ABI, host arrays)"}
+                      "ms_per_step": e2e_s * 1e3, "call": "cg_ (C ABI, host arrays)",
+                      "calls_ms": [round(v, 2) for v in calls],
+                      "clocks": clk_e2e.summary()}
 
     if rank == 0 and world == 1 and not a.no_cpu:
         threads = os.cpu_count() or 1
