@@ -9,8 +9,8 @@ int launch_ax_f64_m2(int lx, AxArgs<double> a, cudaStream_t s);
 int launch_ax_eo_m0(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
 int launch_ax_eo_m1(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
 int launch_ax_eo_m2(int lx, AxArgs<double> a, const double *eo, cudaStream_t s);
-int launch_ax_eo32_m0(int lx, AxArgs<float> a, const float *eo, cudaStream_t s);
-int launch_ax_eo32_m1(int lx, AxArgs<float> a, const float *eo, cudaStream_t s);
+int launch_ax_eo32_m0(int lx, AxArgs<float> a, const double *eo, cudaStream_t s);
+int launch_ax_eo32_m1(int lx, AxArgs<float> a, const double *eo, cudaStream_t s);
 int launch_ax_f32_m0(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m1(int lx, AxArgs<float> a, cudaStream_t s);
 int launch_ax_f32_m2(int lx, AxArgs<float> a, cudaStream_t s);
@@ -19,10 +19,10 @@ template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
-  if (op.order == 1 && op.eo_ok && op.dEO) {  // even-odd split (FP64 pipe bound)
-    if (mode == 0) return launch_ax_eo_m0(op.lx, a, op.dEO, s);
-    if (mode == 1) return launch_ax_eo_m1(op.lx, a, op.dEO, s);
-    return launch_ax_eo_m2(op.lx, a, op.dEO, s);
+  if (op.order == 1 && op.eo_ok) {  // even-odd split (FP64 pipe bound)
+    if (mode == 0) return launch_ax_eo_m0(op.lx, a, op.EO.data(), s);
+    if (mode == 1) return launch_ax_eo_m1(op.lx, a, op.EO.data(), s);
+    return launch_ax_eo_m2(op.lx, a, op.EO.data(), s);
   }
   if (mode == 0) return launch_ax_f64_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f64_m1(op.lx, a, s);
@@ -33,9 +33,9 @@ template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
-  if (op.order == 1 && op.eo_ok && op.fEO && mode != 2) {  // even-odd, one line per thread
-    if (mode == 0) return launch_ax_eo32_m0(op.lx, a, op.fEO, s);
-    return launch_ax_eo32_m1(op.lx, a, op.fEO, s);
+  if (op.order == 1 && op.eo_ok && mode != 2) {  // even-odd, one line per thread
+    if (mode == 0) return launch_ax_eo32_m0(op.lx, a, op.EO.data(), s);
+    return launch_ax_eo32_m1(op.lx, a, op.EO.data(), s);
   }
   if (mode == 0) return launch_ax_f32_m0(op.lx, a, s);
   if (mode == 1) return launch_ax_f32_m1(op.lx, a, s);

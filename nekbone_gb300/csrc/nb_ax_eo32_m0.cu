@@ -2,7 +2,7 @@
 #include "nb_ax_eo_launch.cuh"
 
 namespace nb {
-int launch_ax_eo32_m0(int lx, AxArgs<float> a, const float *eo, cudaStream_t s) {
+int launch_ax_eo32_m0(int lx, AxArgs<float> a, const double *eo, cudaStream_t s) {
   return launch_ax_eo_mode<float, 0>(lx, a, eo, s);
 }
 }  // namespace nb

@@ -439,8 +439,9 @@ struct Batch {
   struct Group {
     int lx = 0, el0 = 0, nel = 0;
     long pt0 = 0, n = 0;
-    double *D64 = nullptr, *EO64 = nullptr;
-    float *D32 = nullptr, *EO32 = nullptr;
+    double *D64 = nullptr;
+    float *D32 = nullptr;
+    std::vector<double> EO;   // even-odd tables (host; empty for odd lx1)
     BatchTune tune;
   };
   int nprob = 0;
@@ -478,8 +479,6 @@ struct Batch {
     for (auto &G : groups) {
       cudaFree(G.D64);
       cudaFree(G.D32);
-      if (G.EO64) cudaFree(G.EO64);
-      if (G.EO32) cudaFree(G.EO32);
     }
     void *ptrs[] = {x, f, g, c, r, w, g32, c32, r32, e32, p32, w32, el_prob, off, gch_g0,
                     gch_prob, pch_prob, cycles, idx, cnt, pch_q0, pb, sc, part_ax, part_gs,
@@ -497,7 +496,7 @@ struct Batch {
       a.g = g32;
       a.c = c32;
       a.D = G.D32;
-      a.eo = G.EO32;
+      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
       a.el_prob = el_prob;
       a.sc = sc;
       a.partial = part_ax;
@@ -517,7 +516,7 @@ struct Batch {
       a.g = g;
       a.c = c;
       a.D = G.D64;
-      a.eo = G.EO64;
+      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
       a.f = f;
       a.r = r;
       a.e = e32;
@@ -793,12 +792,7 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
     std::vector<float> d32(d.begin(), d.end());
     NB_TRY(upload(&G.D64, d));
     NB_TRY(upload(&G.D32, d32));
-    std::vector<double> eo;
-    if (even_odd_tables(d, L, eo)) {
-      std::vector<float> eo32(eo.begin(), eo.end());
-      NB_TRY(upload(&G.EO64, eo));
-      NB_TRY(upload(&G.EO32, eo32));
-    }
+    if (!even_odd_tables(d, L, G.EO)) G.EO.clear();
     // default shape: the first listed (the even-odd form where lx1 is even)
     const auto s32 = batch_shapes_f32(L);
     const auto s64 = batch_shapes_f64(L);
@@ -1007,7 +1001,7 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.g = B.g32;
       a.c = B.c32;
       a.D = G.D32;
-      a.eo = G.EO32;
+      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
       a.el_prob = B.el_prob;
       a.sc = B.sc;
       a.partial = B.part_ax;
@@ -1040,7 +1034,7 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.g = B.g;
       a.c = B.c;
       a.D = G.D64;
-      a.eo = G.EO64;
+      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
       a.f = B.f;
       a.r = B.r;
       a.e = B.e32;

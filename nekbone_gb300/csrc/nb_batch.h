@@ -58,7 +58,8 @@ struct BaxArgs {
   const T *f;          // MODE 2
   T *r;                // MODE 2
   const float *e;      // MODE 2: FP32 correction
-  const T *eo;         // even-odd tables of D (forms with epb 0 / rd 2)
+  const double *eo_h;  // even-odd tables of D on the host (forms with epb 0 /
+                       // rd 2): the launcher passes them as a kernel parameter
   const int *el_prob;  // element -> problem
   const BatchScalars *sc;
   double *partial;     // per element

@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(LX * LX * EPB)
 // bulk copy (FP32).
 template <typename T, int LX, int MODE, bool TMAG>
 __global__ void __launch_bounds__(LX * LX)
-    k_bax_eo(BaxArgs<T> a) {
+    k_bax_eo(BaxArgs<T> a, const __grid_constant__ EoCoef<T, LX> cf) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   AxEoShared<T, LX, TMAG> &sm = *reinterpret_cast<AxEoShared<T, LX, TMAG> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
@@ -254,9 +254,14 @@ __global__ void __launch_bounds__(LX * LX)
     mbar_arrive_expect_tx(&sm.bar, GBYTES);
     bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
   }
-  const T *Ed = sm.E4, *Od = sm.E4 + H * H;
-  const T *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;
-  for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = a.eo[q];
+  // coefficients as in k_ax_eo: FP32 from the parameter bank, FP64 staged
+  // in shared memory
+  constexpr bool CPAR = sizeof(T) == 4 && LX <= 12;
+  if constexpr (!CPAR)
+    for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = cf.c[q];
+  const T *E4 = CPAR ? cf.c : sm.E4;
+  const T *Ed = E4, *Od = E4 + H * H;
+  const T *Et = E4 + 2 * H * H, *Ot = E4 + 3 * H * H;
 
   const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
   T creg[LX], freg[LX];
@@ -398,10 +403,12 @@ int launch_bax_eo(const BaxArgs<T> &a, cudaStream_t s) {
       attr = true;
     }
     if (a.nel <= 0) return NB_OK;
-    if (!a.eo) return fail(NB_ERR_STATE, "batched even-odd operator: no tables");
+    if (!a.eo_h) return fail(NB_ERR_STATE, "batched even-odd operator: no tables");
     if (TMAG && (reinterpret_cast<uintptr_t>(a.g + 6 * a.pt0) & 15u))
       return fail(NB_ERR_STATE, "batched even-odd operator: metric not 16-byte aligned");
-    k_bax_eo<T, LX, MODE, TMAG><<<a.nel, dim3(LX, LX), smem, s>>>(a);
+    EoCoef<T, LX> cf;
+    for (int q = 0; q < 4 * (LX / 2) * (LX / 2); ++q) cf.c[q] = T(a.eo_h[q]);
+    k_bax_eo<T, LX, MODE, TMAG><<<a.nel, dim3(LX, LX), smem, s>>>(a, cf);
     NB_CUDA(cudaGetLastError());
     return NB_OK;
   }

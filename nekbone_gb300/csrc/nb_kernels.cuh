@@ -794,25 +794,34 @@ __device__ __forceinline__ void eo_line(const T *v, const T *Ec, const T *Oc, T 
   }
 }
 
+// The even-odd tables (E, O of D, then E, O of D^T; 4*(lx1/2)^2 values) as
+// a kernel parameter.  Every lane reads the same coefficient at the same
+// time, so from the parameter bank they are operands of the FMAs
+// themselves; from shared memory each one was a broadcast load.
+template <typename T, int LX>
+struct EoCoef {
+  T c[4 * (LX / 2) * (LX / 2)];
+};
+
 template <typename T, int LX, int MODE, bool TMAG>
-__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const T *eo);
+__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, LX> &cf);
 
 template <typename T, int LX, int MODE, bool TMAG>
 __global__ void __launch_bounds__(LX * LX)
-    k_ax_eo(AxArgs<T> a, const T *eo) {
-  ax_eo_body<T, LX, MODE, TMAG>(a, eo);
+    k_ax_eo(AxArgs<T> a, const __grid_constant__ EoCoef<T, LX> cf) {
+  ax_eo_body<T, LX, MODE, TMAG>(a, cf);
 }
 // The same with four CTAs per SM asked for (the FP64 lx1 = 12 operator):
 // the FP64 pipe is its bound, and a fourth CTA's warps cover the barrier
 // and shared-memory waits
 template <typename T, int LX, int MODE, bool TMAG>
 __global__ void __launch_bounds__(LX * LX, 4)
-    k_ax_eo4(AxArgs<T> a, const T *eo) {
-  ax_eo_body<T, LX, MODE, TMAG>(a, eo);
+    k_ax_eo4(AxArgs<T> a, const __grid_constant__ EoCoef<T, LX> cf) {
+  ax_eo_body<T, LX, MODE, TMAG>(a, cf);
 }
 
 template <typename T, int LX, int MODE, bool TMAG>
-__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const T *eo) {
+__device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, LX> &cf) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   AxEoShared<T, LX, TMAG> &sm = *reinterpret_cast<AxEoShared<T, LX, TMAG> *>(smem_raw);
   constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
@@ -828,10 +837,16 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const T *eo) {
     mbar_arrive_expect_tx(&sm.bar, GBYTES);
     bulk_g2s(sm.g, gblk, GBYTES, &sm.bar);
   }
-  const T *Ed = sm.E4, *Od = sm.E4 + H * H;            // of D
-  const T *Et = sm.E4 + 2 * H * H, *Ot = sm.E4 + 3 * H * H;  // of D^T
-
-  for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = eo[q];
+  // FP32 up to lx1 = 12 reads the coefficients from the parameter bank.
+  // FP64 and the larger FP32 shapes copy them to shared memory: from the
+  // parameter bank the compiler keeps many of them in registers, and those
+  // forms spill (FP64) or double their registers (FP32, lx1 = 16).
+  constexpr bool CPAR = sizeof(T) == 4 && LX <= 12;
+  if constexpr (!CPAR)
+    for (int q = t; q < 4 * H * H; q += L2) sm.E4[q] = cf.c[q];
+  const T *E4 = CPAR ? cf.c : sm.E4;
+  const T *Ed = E4, *Od = E4 + H * H;                // of D
+  const T *Et = E4 + 2 * H * H, *Ot = E4 + 3 * H * H;  // of D^T
 
   const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
   T creg[LX], freg[LX];

@@ -20,8 +20,6 @@
 namespace nb {
 
 Operator::~Operator() {
-  if (dEO) cudaFree(dEO);
-  if (fEO) cudaFree(fEO);
   if (dD) cudaFree(dD);
   if (fD) cudaFree(fD);
   gs_release(&gs);
@@ -276,19 +274,7 @@ int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
   NB_CUDA(cudaMemcpy(op->dD, op->D.data(), lx * lx * sizeof(double), cudaMemcpyHostToDevice));
   NB_CUDA(cudaMemcpy(op->fD, fDh.data(), lx * lx * sizeof(float), cudaMemcpyHostToDevice));
   // even-odd tables when D(n-1-i,n-1-m) = -D(i,m) holds to rounding
-  {
-    std::vector<double> eo;
-    if (even_odd_tables(op->D, lx, eo)) {
-      NB_CUDA(cudaMalloc(&op->dEO, eo.size() * sizeof(double)));
-      NB_CUDA(cudaMemcpy(op->dEO, eo.data(), eo.size() * sizeof(double),
-                         cudaMemcpyHostToDevice));
-      std::vector<float> eo32(eo.begin(), eo.end());
-      NB_CUDA(cudaMalloc(&op->fEO, eo32.size() * sizeof(float)));
-      NB_CUDA(cudaMemcpy(op->fEO, eo32.data(), eo32.size() * sizeof(float),
-                         cudaMemcpyHostToDevice));
-      op->eo_ok = true;
-    }
-  }
+  op->eo_ok = even_odd_tables(op->D, lx, op->EO);
   op->face.resize(nelt);
   for (int e = 0; e < nelt; ++e)
     op->face[e] = (unsigned char)face_bits(op->lglel[e], nelx, nely, nelz);

@@ -18,10 +18,10 @@ struct Operator {
   std::vector<double> D;           // dxm1, column-major
   double *dD = nullptr;
   float *fD = nullptr;
-  // even-odd split of D (E, O of D and of D^T, 4*(lx/2)^2); valid when lx is
+  // even-odd split of D (E, O of D and of D^T, 4*(lx/2)^2), kept on the
+  // host: each launch passes them as a kernel parameter.  Valid when lx is
   // even and D is anti-centrosymmetric to rounding
-  double *dEO = nullptr;
-  float *fEO = nullptr;            // the same tables in FP32
+  std::vector<double> EO;
   bool eo_ok = false;
   int order = 1;                   // 0 reference left-to-right sums, 1 even-odd
                                    // (FP64 and FP32 operators alike)
