@@ -66,9 +66,10 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--cpu-sample-nel", type=int, default=16)
     ap.add_argument("--cpu-sample-iters", type=int, default=250)
-    ap.add_argument("--case", choices=["cg", "tc", "batch", "hsmg"], default="cg",
-                    help="cg: the benchmark; tc / batch / hsmg: a small case of the "
-                         "tensor-core operator / the batched solver / hsmg PCG, for profiling")
+    ap.add_argument("--case", choices=["cg", "tc", "batch", "hsmg", "mixed"], default="cg",
+                    help="cg: the benchmark; tc / batch / hsmg / mixed: a small case of the "
+                         "tensor-core operator / the batched solver / hsmg PCG / the mixed "
+                         "solver, for profiling")
     return ap.parse_args()
 
 
@@ -583,7 +584,9 @@ def run_case(a):
     deformed elements (lx1 = --lx); 'batch' solves the first 32 problems of
     the batched workload once after tuning; 'hsmg' runs 6 PCG iterations with
     the FP32-smoother V-cycle (levels 12 -> 6 -> 2 points, exact coarse solve)
-    on 16^3 deformed elements, lx1 = 12."""
+    on 16^3 deformed elements, lx1 = 12; 'mixed' runs one mixed-precision
+    solve (20 FP32 inner iterations per cycle) to 1e-10 on the --nel^3 box,
+    lx1 = --lx."""
     import torch
     import nekbone_gb300 as nb
     dev = torch.device("cuda", 0)
@@ -620,6 +623,23 @@ def run_case(a):
         it, rr = m.pcg_tol(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), 1e-10,
                            max_iter=6, check_every=6)
         out = {"case": "hsmg", "n": n, "iters": it, "relres": rr,
+               "s": time.perf_counter() - t0}
+        m.close()
+    elif a.case == "mixed":
+        m = nb.DeviceMesh(a.nel, a.nel, a.nel, a.lx, mask_mode=1)
+        n = m.n
+        g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+        c = torch.empty(n, dtype=torch.float64, device=dev)
+        f = torch.empty(n, dtype=torch.float64, device=dev)
+        m.setup_g(g.data_ptr())
+        m.set_multiplicity(c.data_ptr())
+        m.rhs_uniform(f.data_ptr(), c.data_ptr(), 20260)
+        x = torch.zeros_like(f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outer, inner, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
+                                      a.tol, 20, 500)
+        out = {"case": "mixed", "n": n, "outer": outer, "inner": inner, "relres": rr,
                "s": time.perf_counter() - t0}
         m.close()
     else:

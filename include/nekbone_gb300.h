@@ -183,6 +183,12 @@ int nb_mesh_boundary_groups(const nb_mesh *mesh, int *nbg, long *nmem, int *off,
                             unsigned *idx);
 /* The mesh's masked local indices (ascending). */
 int nb_mesh_mask_list(const nb_mesh *mesh, int *n, int *list);
+/* The FP32 even-odd operator's line order for lx1 (even, 2..12): the r-line
+ * (j + lx1 k) and s-line (i + lx1 k) that thread t of the lx1^2-thread CTA
+ * takes, dealt so that each warp's lines start in distinct shared-memory
+ * banks where the counts allow; *plane = the layout's plane stride in words
+ * (rows are lx1 words).  rmap and smap hold lx1^2 entries. */
+int nb_eo_line_maps(int lx1, int *plane, unsigned char *rmap, unsigned char *smap);
 /* contraction order of this mesh's FP64 operator (see
  * nekbone_set_contraction_order_) */
 int  nb_mesh_set_order(nb_mesh *mesh, int order);

@@ -55,7 +55,7 @@ EXPORTS = (
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_set_inner_tol", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
-    "nb_mg_setup_coarse",
+    "nb_mg_setup_coarse", "nb_eo_line_maps",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -132,6 +132,8 @@ lib.nb_mg_setup_coarse.restype = _i
 lib.nb_mg_setup_coarse.argtypes = [_p, _p]
 lib.nb_mesh_mask_list.restype = _i
 lib.nb_mesh_mask_list.argtypes = [_p, _p, _p]
+lib.nb_eo_line_maps.restype = _i
+lib.nb_eo_line_maps.argtypes = [_i, _p, _p, _p]
 #: largest n nb_glsc3_noalloc accepts (its fixed scratch holds the partials)
 NOALLOC_MAX_N = 67108864
 
@@ -625,6 +627,17 @@ def set_setup_on_device(on: bool) -> None:
 def set_mg_fixed_kernels(on: bool) -> None:
     """hsmg: fixed-size FDM/transfer kernels (default) or the general ones."""
     lib.nb_set_mg_fixed_kernels(1 if on else 0)
+
+
+def eo_line_maps(lx1: int):
+    """The FP32 even-odd operator's line order for lx1: (plane stride,
+    r-line map, s-line map); thread t takes r-line rmap[t] = j + lx1 k and
+    s-line smap[t] = i + lx1 k."""
+    pl = _C.c_int()
+    r = _np.zeros(lx1 * lx1, dtype=_np.uint8)
+    s_ = _np.zeros(lx1 * lx1, dtype=_np.uint8)
+    _check(lib.nb_eo_line_maps(lx1, _C.byref(pl), _ptr(r), _ptr(s_)))
+    return pl.value, r, s_
 
 
 def set_shared_metric(on: bool) -> None:

@@ -815,6 +815,24 @@ int nb_mesh_create(nb_mesh **mesh, int nelx, int nely, int nelz, int lx1,
 void nb_set_setup_on_device(int on) { set_setup_on_device(on != 0); }
 void nb_set_mg_fixed_kernels(int on) { mg_set_fixed_kernels(on != 0); }
 
+int nb_eo_line_maps(int lx1, int *plane, unsigned char *rmap, unsigned char *smap) {
+  clear_status();
+  int pl = 0;
+  switch (lx1) {
+    case 2: pl = eo_plane<float, 2>(); break;
+    case 4: pl = eo_plane<float, 4>(); break;
+    case 6: pl = eo_plane<float, 6>(); break;
+    case 8: pl = eo_plane<float, 8>(); break;
+    case 10: pl = eo_plane<float, 10>(); break;
+    case 12: pl = eo_plane<float, 12>(); break;
+    default: return fail(NB_ERR_ARG, "nb_eo_line_maps: lx1=%d (even, 2..12)", lx1);
+  }
+  if (!rmap || !smap) return fail(NB_ERR_ARG, "nb_eo_line_maps: null map");
+  if (plane) *plane = pl;
+  eo_line_maps(lx1, pl, rmap, smap);
+  return NB_OK;
+}
+
 // Copies one device int array (count entries) to host, when dst is given.
 static int copy_out(void *dst, const void *src, size_t bytes) {
   if (!dst || !bytes) return NB_OK;

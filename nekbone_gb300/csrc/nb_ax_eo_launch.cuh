@@ -24,7 +24,7 @@ int launch_ax_eo_shape(AxArgs<T> a, const double *eo, cudaStream_t s) {
     attr_set = true;
   }
   EoCoef<T, LX> cf;
-  for (int q = 0; q < 4 * (LX / 2) * (LX / 2); ++q) cf.c[q] = T(eo[q]);
+  eo_fill(cf, eo);
   fn<<<a.nelt, dim3(LX, LX), sm, s>>>(a, cf);
   NB_CUDA(cudaGetLastError());
   return NB_OK;

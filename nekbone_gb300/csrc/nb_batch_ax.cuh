@@ -263,6 +263,10 @@ __global__ void __launch_bounds__(LX * LX)
   const T *Ed = E4, *Od = E4 + H * H;
   const T *Et = E4 + 2 * H * H, *Ot = E4 + 3 * H * H;
 
+  constexpr bool DEALT = eo_dealt<T, LX>();
+  const int lr = DEALT ? int(cf.rmap[t]) : t, ls = DEALT ? int(cf.smap[t]) : t;
+  const int r0 = lr % LX, r1 = lr / LX, s0 = ls % LX, s1 = ls / LX;
+
   const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
   T creg[LX], freg[LX];
   if (col_interior) {
@@ -296,22 +300,21 @@ __global__ void __launch_bounds__(LX * LX)
       ureg[k] = fma_rn(scale, pold[k], ureg[k]);
     }
     a.p[id] = ureg[k];
-    sm.A[eo_at<LX>(i, j, k)] = ureg[k];
+    sm.A[eo_at<T, LX>(i, j, k)] = ureg[k];
   }
   __syncthreads();
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(m, l0, l1)];
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<T, LX>(m, r0, r1)];
     eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(m, l0, l1)] = y[m];
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<T, LX>(m, r0, r1)] = y[m];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(l0, m, l1)];
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<T, LX>(s0, m, s1)];
     eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.C[eo_at<LX>(l0, m, l1)] = y[m];
+    for (int m = 0; m < LX; ++m) sm.C[eo_at<T, LX>(s0, m, s1)] = y[m];
   }
   T wtreg[LX];
   eo_line<T, LX>(ureg, Ed, Od, wtreg);
@@ -319,7 +322,7 @@ __global__ void __launch_bounds__(LX * LX)
   if (TMAG) mbar_wait_bounded(&sm.bar, 0, nullptr);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
-    const int q = eo_at<LX>(i, j, k);
+    const int q = eo_at<T, LX>(i, j, k);
     const T ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
     const size_t pt = base + size_t(k) * L2 + t;
     typedef typename Vec2<T>::type V2;
@@ -341,23 +344,21 @@ __global__ void __launch_bounds__(LX * LX)
   }
   __syncthreads();
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<LX>(m, l0, l1)];
+    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<T, LX>(m, r0, r1)];
     eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.A[eo_at<LX>(m, l0, l1)] = y[m];
+    for (int m = 0; m < LX; ++m) sm.A[eo_at<T, LX>(m, r0, r1)] = y[m];
   }
   __syncthreads();
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<LX>(l0, m, l1)];
+    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<T, LX>(s0, m, s1)];
     eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(l0, m, l1)] = y[m];
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<T, LX>(s0, m, s1)] = y[m];
   }
   T ttreg[LX];
   eo_line<T, LX>(wtreg, Et, Ot, ttreg);
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(LX * LX)
   T part = T(0);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
-    const int q = eo_at<LX>(i, j, k);
+    const int q = eo_at<T, LX>(i, j, k);
     T wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
     const size_t id = base + size_t(k) * L2 + t;
     const bool interior = col_interior && (k > 0) && (k < LX - 1);
@@ -407,7 +408,7 @@ int launch_bax_eo(const BaxArgs<T> &a, cudaStream_t s) {
     if (TMAG && (reinterpret_cast<uintptr_t>(a.g + 6 * a.pt0) & 15u))
       return fail(NB_ERR_STATE, "batched even-odd operator: metric not 16-byte aligned");
     EoCoef<T, LX> cf;
-    for (int q = 0; q < 4 * (LX / 2) * (LX / 2); ++q) cf.c[q] = T(a.eo_h[q]);
+    eo_fill(cf, a.eo_h);
     k_bax_eo<T, LX, MODE, TMAG><<<a.nel, dim3(LX, LX), smem, s>>>(a, cf);
     NB_CUDA(cudaGetLastError());
     return NB_OK;

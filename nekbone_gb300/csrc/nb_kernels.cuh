@@ -752,10 +752,33 @@ namespace nb {
 // the CTA starts, instead of per-point loads in the metric step -- the FP32
 // form, where those loads would otherwise wait on DRAM latency one plane at
 // a time.
+// Shared-memory layout of the even-odd kernels.  The FP32 forms up to
+// lx1 = 12 keep rows unpadded, so a warp's column accesses (7 per point)
+// touch 32 consecutive words, and space the planes eo_plane words apart;
+// their r- and s-line phases take the lines in the order of EoCoef's maps,
+// which deal each warp lines that start in distinct banks.  The other forms
+// pad rows to lx1 + 1 and take lines in natural order.
+template <typename T, int LX>
+constexpr bool eo_dealt() { return sizeof(T) == 4 && LX <= 12; }
+
+template <typename T, int LX>
+constexpr int eo_plane() {
+  if constexpr (eo_dealt<T, LX>()) {
+    // plane strides with the fewest conflicts of the dealt lines
+    return LX == 12 ? 145 : LX == 10 ? 103 : LX == 8 ? 71 : LX == 6 ? 47 : LX == 4 ? 19 : LX * LX;
+  } else {
+    return (LX + 1) * LX;
+  }
+}
+
+template <typename T, int LX>
+__device__ __forceinline__ int eo_at(int i, int j, int k) {
+  return i + (eo_dealt<T, LX>() ? LX : LX + 1) * j + eo_plane<T, LX>() * k;
+}
+
 template <typename T, int LX, bool TMAG>
 struct AxEoShared {
-  static constexpr int P = LX + 1;
-  static constexpr int N = P * LX * LX;
+  static constexpr int N = eo_plane<T, LX>() * LX;
   alignas(128) T g[TMAG ? 6 * LX * LX * LX : 2];
   T A[N];
   T B[N];
@@ -765,10 +788,6 @@ struct AxEoShared {
   double red[32];
 };
 
-template <int LX>
-__device__ __forceinline__ int eo_at(int i, int j, int k) {
-  return i + (LX + 1) * j + (LX + 1) * LX * k;
-}
 
 // y(0..n-1) of a folded line v (length n), coefficients Ec/Oc (h x h, row a)
 template <typename T, int LX>
@@ -798,10 +817,39 @@ __device__ __forceinline__ void eo_line(const T *v, const T *Ec, const T *Oc, T 
 // a kernel parameter.  Every lane reads the same coefficient at the same
 // time, so from the parameter bank they are operands of the FMAs
 // themselves; from shared memory each one was a broadcast load.
+// rmap / smap (FP32 forms up to lx1 = 12): the r-line (j, k) and s-line
+// (i, k) that thread t takes, as j + lx1 k and i + lx1 k (eo_line_maps).
 template <typename T, int LX>
 struct EoCoef {
   T c[4 * (LX / 2) * (LX / 2)];
+  unsigned char rmap[LX * LX], smap[LX * LX];
 };
+
+// The line maps of an lx1^2-thread CTA whose planes are pl words apart
+// (nb_solver.cu).
+void eo_line_maps(int lx, int pl, unsigned char *rmap, unsigned char *smap);
+
+// A launch's EoCoef: the tables eo (FP64, host) rounded to T, and the line
+// maps of the form's layout (identity for the forms that do not deal lines).
+template <typename T, int LX>
+void eo_fill(EoCoef<T, LX> &cf, const double *eo) {
+  struct Maps {
+    unsigned char r[LX * LX], s[LX * LX];
+    Maps() {
+      if (eo_dealt<T, LX>()) {
+        eo_line_maps(LX, eo_plane<T, LX>(), r, s);
+      } else {
+        for (int t = 0; t < LX * LX; ++t) r[t] = s[t] = (unsigned char)t;
+      }
+    }
+  };
+  static const Maps maps;
+  for (int q = 0; q < 4 * (LX / 2) * (LX / 2); ++q) cf.c[q] = T(eo[q]);
+  for (int t = 0; t < LX * LX; ++t) {
+    cf.rmap[t] = maps.r[t];
+    cf.smap[t] = maps.s[t];
+  }
+}
 
 template <typename T, int LX, int MODE, bool TMAG>
 __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, LX> &cf);
@@ -848,6 +896,11 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
   const T *Ed = E4, *Od = E4 + H * H;                // of D
   const T *Et = E4 + 2 * H * H, *Ot = E4 + 3 * H * H;  // of D^T
 
+  // the r-line (r0 = j, r1 = k) and s-line (s0 = i, s1 = k) of this thread
+  constexpr bool DEALT = eo_dealt<T, LX>();
+  const int lr = DEALT ? int(cf.rmap[t]) : t, ls = DEALT ? int(cf.smap[t]) : t;
+  const int r0 = lr % LX, r1 = lr / LX, s0 = ls % LX, s1 = ls / LX;
+
   const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
   T creg[LX], freg[LX];
   if (MODE != 0 && col_interior) {
@@ -883,24 +936,23 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
       ureg[k] = fma_rn(T(a.scale), pold[k], ureg[k]);
       a.p[id] = ureg[k];
     }
-    sm.A[eo_at<LX>(i, j, k)] = ureg[k];
+    sm.A[eo_at<T, LX>(i, j, k)] = ureg[k];
   }
   __syncthreads();
 
   // gradient (local_grad3, cg.f:170-187) as three folded contractions
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(m, l0, l1)];  // line (j,k)
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<T, LX>(m, r0, r1)];  // line (j,k)
     eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(m, l0, l1)] = y[m];  // ur
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<T, LX>(m, r0, r1)] = y[m];  // ur
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<LX>(l0, m, l1)];  // line (i,k)
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[eo_at<T, LX>(s0, m, s1)];  // line (i,k)
     eo_line<T, LX>(v, Ed, Od, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.C[eo_at<LX>(l0, m, l1)] = y[m];  // us
+    for (int m = 0; m < LX; ++m) sm.C[eo_at<T, LX>(s0, m, s1)] = y[m];  // us
   }
   T wtreg[LX];
   eo_line<T, LX>(ureg, Ed, Od, wtreg);  // ut of the own column
@@ -910,7 +962,7 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
   if (TMAG) mbar_wait_bounded(&sm.bar, 0, a.err);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
-    const int q = eo_at<LX>(i, j, k);
+    const int q = eo_at<T, LX>(i, j, k);
     const T ur = sm.B[q], us = sm.C[q], ut = wtreg[k];
     typedef typename Vec2<T>::type V2;
     const V2 *gp = TMAG ? reinterpret_cast<const V2 *>(&sm.g[6 * (k * L2 + t)])
@@ -933,23 +985,21 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
 
   // transposed gradient (local_grad3_t, cg.f:189-212) with D^T
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<LX>(m, l0, l1)];  // wr line (j,k)
+    for (int m = 0; m < LX; ++m) v[m] = sm.B[eo_at<T, LX>(m, r0, r1)];  // wr line (j,k)
     eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.A[eo_at<LX>(m, l0, l1)] = y[m];  // tr
+    for (int m = 0; m < LX; ++m) sm.A[eo_at<T, LX>(m, r0, r1)] = y[m];  // tr
   }
   __syncthreads();
   {
-    const int l0 = t % LX, l1 = t / LX;
     T v[LX], y[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<LX>(l0, m, l1)];  // ws line (i,k)
+    for (int m = 0; m < LX; ++m) v[m] = sm.C[eo_at<T, LX>(s0, m, s1)];  // ws line (i,k)
     eo_line<T, LX>(v, Et, Ot, y);
 #pragma unroll
-    for (int m = 0; m < LX; ++m) sm.B[eo_at<LX>(l0, m, l1)] = y[m];  // ts
+    for (int m = 0; m < LX; ++m) sm.B[eo_at<T, LX>(s0, m, s1)] = y[m];  // ts
   }
   T ttreg[LX];
   eo_line<T, LX>(wtreg, Et, Ot, ttreg);
@@ -958,7 +1008,7 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
   T part = T(0);
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
-    const int q = eo_at<LX>(i, j, k);
+    const int q = eo_at<T, LX>(i, j, k);
     T wl = add_rn(add_rn(sm.A[q], sm.B[q]), ttreg[k]);
     const size_t id = base + size_t(k) * L2 + t;
     const bool interior = col_interior && (k > 0) && (k < LX - 1);

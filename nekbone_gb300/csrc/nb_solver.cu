@@ -117,6 +117,70 @@ bool even_odd_tables(const std::vector<double> &D, int lx, std::vector<double> &
   return true;
 }
 
+// Deals the lx^2 lines of one phase (line l starts in bank bank[l]) to the
+// CTA's warps, 32 lanes each: a transportation problem from banks to warps,
+// solved by max-flow with a per-(bank, warp) limit.  The limit starts at
+// one line per bank in every warp and is raised one warp at a time until
+// every line is placed.
+static void deal_lines(int nt, const std::vector<int> &bank, unsigned char *map) {
+  const int W = (nt + 31) / 32, N = 34 + W;  // 0 source, 1 sink, 2.. banks, 34.. warps
+  std::vector<int> cnt(32, 0);
+  for (int l = 0; l < nt; ++l) cnt[bank[l]]++;
+  for (int extra = 0;; ++extra) {
+    std::vector<int> cap(size_t(N) * N, 0);
+    auto C = [&](int u, int v) -> int & { return cap[size_t(u) * N + v]; };
+    for (int b = 0; b < 32; ++b) {
+      C(0, 2 + b) = cnt[b];
+      for (int w = 0; w < W; ++w) C(2 + b, 34 + w) = 1 + extra / W + (w < extra % W ? 1 : 0);
+    }
+    for (int w = 0; w < W; ++w) C(34 + w, 1) = std::min(32, nt - 32 * w);
+    int flow = 0;
+    for (;;) {
+      std::vector<int> par(N, -1), q(1, 0);
+      par[0] = 0;
+      for (size_t h = 0; h < q.size() && par[1] < 0; ++h)
+        for (int v = 0; v < N; ++v)
+          if (par[v] < 0 && C(q[h], v) > 0) {
+            par[v] = q[h];
+            q.push_back(v);
+          }
+      if (par[1] < 0) break;
+      int m = nt;
+      for (int v = 1; v != 0; v = par[v]) m = std::min(m, C(par[v], v));
+      for (int v = 1; v != 0; v = par[v]) {
+        C(par[v], v) -= m;
+        C(v, par[v]) += m;
+      }
+      flow += m;
+    }
+    if (flow != nt) continue;
+    // the flow from bank b to warp w sits on the reverse edge
+    std::vector<int> fill(W, 0);
+    for (int l = 0; l < nt; ++l) {
+      const int b = bank[l];
+      for (int w = 0; w < W; ++w)
+        if (C(34 + w, 2 + b) > 0) {
+          C(34 + w, 2 + b)--;
+          map[32 * w + fill[w]++] = (unsigned char)l;
+          break;
+        }
+    }
+    return;
+  }
+}
+
+void eo_line_maps(int lx, int pl, unsigned char *rmap, unsigned char *smap) {
+  const int nt = lx * lx;
+  std::vector<int> br(nt), bs(nt);
+  for (int k = 0; k < lx; ++k)
+    for (int a = 0; a < lx; ++a) {
+      br[a + lx * k] = (lx * a + pl * k) % 32;  // r-line (j = a, k): word j lx + k pl
+      bs[a + lx * k] = (a + pl * k) % 32;       // s-line (i = a, k): word i + k pl
+    }
+  deal_lines(nt, br, rmap);
+  deal_lines(nt, bs, smap);
+}
+
 static bool is_elem_boundary(long pt, int lx) {
   const long l3 = long(lx) * lx * lx;
   const int r = int(pt % l3);

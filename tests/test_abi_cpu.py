@@ -105,3 +105,51 @@ def test_get_exyz_brick_positions(dims):
         assert ex + nelx * (ey - 1) + nelx * nely * (ez - 1) == eg
         seen.add((ex, ey, ez))
     assert len(seen) == nelx * nely * nelz
+
+
+def _warp_wavefronts(starts, nt):
+    """Shared-memory wavefronts of one line phase: per warp, the most lines
+    whose first words share a bank (4-byte words, 32 banks)."""
+    total = 0
+    for w in range(0, nt, 32):
+        banks = {}
+        for s in starts[w:w + 32]:
+            banks[s % 32] = banks.get(s % 32, 0) + 1
+        total += max(banks.values())
+    return total
+
+
+# (lx1, r-line wavefronts, s-line wavefronts) the dealt order reaches; the
+# bound is one per warp where every bank holds at most one line per warp
+DEALT_COST = [(2, 1, 1), (4, 1, 1), (6, 2, 3), (8, 2, 3), (10, 5, 5), (12, 5, 6)]
+
+
+@pytest.mark.parametrize("lx,cr,cs", DEALT_COST)
+def test_eo_line_maps_deal_lines_to_distinct_banks(lx, cr, cs):
+    import nekbone_gb300 as nb
+    pl, rmap, smap = nb.eo_line_maps(lx)
+    nt = lx * lx
+    assert pl >= lx * lx
+    assert sorted(rmap.tolist()) == list(range(nt))
+    assert sorted(smap.tolist()) == list(range(nt))
+    # first word of r-line (j, k): j lx + k pl; of s-line (i, k): i + k pl
+    rs = [(l % lx) * lx + (l // lx) * pl for l in rmap.tolist()]
+    ss = [(l % lx) + (l // lx) * pl for l in smap.tolist()]
+    assert _warp_wavefronts(rs, nt) <= cr
+    assert _warp_wavefronts(ss, nt) <= cs
+    # against the rows-padded layout in natural order, weighting each phase
+    # by its accesses per point (7 column accesses, 4 r-line, 4 s-line)
+    nat = list(range(nt))
+    col_new = _warp_wavefronts(nat, nt)                 # thread (i, j): word i + lx j
+    col_pad = _warp_wavefronts([(t % lx) + (t // lx) * (lx + 1) for t in nat], nt)
+    r_pad = _warp_wavefronts([(l % lx) * (lx + 1) + (l // lx) * (lx + 1) * lx for l in nat], nt)
+    s_pad = _warp_wavefronts([(l % lx) + (l // lx) * (lx + 1) * lx for l in nat], nt)
+    assert col_new == (nt + 31) // 32
+    assert 7 * col_new + 4 * (cr + cs) <= 7 * col_pad + 4 * (r_pad + s_pad)
+
+
+def test_eo_line_maps_rejects_bad_orders():
+    import nekbone_gb300 as nb
+    for lx in (3, 14, 0):
+        with pytest.raises(nb.NekboneError):
+            nb.eo_line_maps(lx)
