@@ -524,6 +524,24 @@ def run_ours(a, rank, world, local):
         out["mixed"] = {"tol": a.tol, "fp64_s": t64, "fp64_iters": it64, "fp64_relres": rr64,
                         "mixed_s": tm, "mixed_outer": outer, "mixed_inner_iters": inner,
                         "mixed_relres": rrm, "speedup": t64 / tm, "x_rel_diff": diff}
+        # the same solve with the inner element products on the tensor cores
+        # (FP16 hi+lo split operands, FP32 accumulation; unfused iteration)
+        nb.set_mixed_tensor_cores(True)
+        try:
+            xm.zero_()
+            mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol, 20, 5000)
+            xm.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            o_tc, i_tc, rr_tc = mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(),
+                                              c.data_ptr(), a.tol, 20, 5000)
+            t_tc = time.perf_counter() - t0
+        finally:
+            nb.set_mixed_tensor_cores(False)
+        d_tc = float((xm - xt).abs().max().item() / max(xt.abs().max().item(), 1e-300))
+        out["mixed"]["tensor_cores"] = {"s": t_tc, "outer": o_tc, "inner_iters": i_tc,
+                                        "relres": rr_tc, "speedup_vs_fp64": t64 / t_tc,
+                                        "x_rel_diff": d_tc}
         del xt, xm
 
     # ---- the other workloads, one measurement each (not the headline)

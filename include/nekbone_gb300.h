@@ -173,6 +173,12 @@ void nb_set_mg_fixed_kernels(int on);
  * operator reads that one block instead of each element's; 0 always reads
  * each element's.  Same values either way (bitwise-equal results). */
 void nb_set_shared_metric(int on);
+/* Mixed solver: 1 takes the inner FP32 CG's element products on the tensor
+ * cores (nb_ax_tc's operator: FP16 hi+lo split operands, FP32
+ * accumulation), each iteration unfused (operator, gather-scatter, dot
+ * products, update); 0 (default) the fused CUDA-core iteration.  The FP64
+ * defect correction is the same either way, so both reach the tolerance. */
+void nb_set_mixed_tensor_cores(int on);
 /* The mesh's gather-scatter groups (jl order: groups by primary, members
  * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)
  * are filled when given. */

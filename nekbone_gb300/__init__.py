@@ -55,7 +55,7 @@ EXPORTS = (
     "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_set_inner_tol", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
-    "nb_mg_setup_coarse", "nb_eo_line_maps",
+    "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -125,6 +125,8 @@ lib.nb_set_mg_fixed_kernels.restype = None
 lib.nb_set_mg_fixed_kernels.argtypes = [_i]
 lib.nb_set_shared_metric.restype = None
 lib.nb_set_shared_metric.argtypes = [_i]
+lib.nb_set_mixed_tensor_cores.restype = None
+lib.nb_set_mixed_tensor_cores.argtypes = [_i]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
@@ -638,6 +640,12 @@ def eo_line_maps(lx1: int):
     s_ = _np.zeros(lx1 * lx1, dtype=_np.uint8)
     _check(lib.nb_eo_line_maps(lx1, _C.byref(pl), _ptr(r), _ptr(s_)))
     return pl.value, r, s_
+
+
+def set_mixed_tensor_cores(on: bool) -> None:
+    """Mixed solver: the inner CG's element products on the tensor cores
+    (True) or the fused CUDA-core iteration (False, default)."""
+    lib.nb_set_mixed_tensor_cores(1 if on else 0)
 
 
 def set_shared_metric(on: bool) -> None:

@@ -37,7 +37,6 @@ int dev_rhs_uniform(const Operator &op, double *f, const double *c,
                     uint64_t seed, cudaStream_t s);
 int dev_setup_g_deformed(const Operator &op, double *g, uint64_t seed, double amp,
                          cudaStream_t s);
-int apply_ax_tc(const Operator &op, float *w, const float *u, const float *g, cudaStream_t s);
 int dev_residual(const Operator &op, double *r, const double *f,
                  const double *w, long n, cudaStream_t s);
 int dev_axpy_f32(double *x, const float *e, double scale, long n, cudaStream_t s);

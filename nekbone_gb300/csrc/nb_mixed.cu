@@ -204,6 +204,9 @@ __global__ void k_metric_uniform(const unsigned *g, long blk, long nelt, int *sa
 // with the same values, so the same results.
 bool g_shared_metric = true;
 void set_shared_metric(bool on) { g_shared_metric = on; }
+// the inner CG's element products on the tensor cores (k_ax_tc: FP16 hi+lo
+// split operands, FP32 accumulation) instead of the fused CUDA-core pass
+bool g_mixed_tc = false;
 
 // flag: one device int of scratch
 int metric_uniform(const float *g32, long nelt, int lx, int *flag, int *uniform,
@@ -230,6 +233,7 @@ int metric_uniform(const float *g32, long nelt, int lx, int *flag, int *uniform,
 extern "C" {
 
 void nb_set_shared_metric(int on) { set_shared_metric(on != 0); }
+void nb_set_mixed_tensor_cores(int on) { g_mixed_tc = on != 0; }
 
 int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
                 const double *c, double tol, int inner_iters, int max_outer,
@@ -278,8 +282,10 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     // inner FP32 solve of A e = r / |r|
     st = dev_scale_to_f32(r32, r, 1.0 / rn, n, s);
     wk.g32_uniform = uniform;
+    wk.tc_inner = g_mixed_tc;
     if (!st) st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s);
     wk.g32_uniform = 0;
+    wk.tc_inner = false;
     // FP64 defect: x += |r| e; r = f - A x; r'Cr
     if (!st && fused) {
       st = residual_fused(op, wk, x, e32, rn, f, g, c, r, w, s);

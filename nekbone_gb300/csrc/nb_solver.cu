@@ -568,7 +568,8 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
                       Precond *M, bool force_unfused, cudaStream_t s) {
   const long n = op.n;
   const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
-  const bool fused = op.fused_ok && !force_unfused;
+  const bool tc = std::is_same<T, float>::value && wk.tc_inner;
+  const bool fused = op.fused_ok && !force_unfused && !tc;
   for (int iter = it0; iter <= it1; ++iter) {
     T *zz = r;
     if (M) {
@@ -611,7 +612,12 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
         k_copy_first<T><<<grid_for(n), 256, 0, s>>>(p, zz, n);
       else
         NB_TRY(vec_add2s1<T>(p, zz, &wk.sc->beta, 0.0, n, s));
-      NB_TRY(apply_ax<T>(op, w, p, g, s));
+      if constexpr (std::is_same<T, float>::value) {
+        if (tc) NB_TRY(apply_ax_tc(op, w, p, g, s));
+        else NB_TRY(apply_ax<T>(op, w, p, g, s));
+      } else {
+        NB_TRY(apply_ax<T>(op, w, p, g, s));
+      }
       NB_TRY(vec_glsc3<T>(w, c, p, n, wk, wk.dot_out + 2, nullptr, 0, iter, s));
       k_set_alpha<<<1, 1, 0, s>>>(wk.sc, wk.dot_out + 2);
       NB_CUDA(cudaGetLastError());

@@ -68,6 +68,9 @@ struct CgWork {
   int g32_uniform = 0;
   // the preconditioner's FP32 input holds float(r) of the current r
   bool r32_ready = false;
+  // an FP32 solve in progress takes its element products on the tensor
+  // cores (unfused iteration; set by the mixed solver around its inner CG)
+  bool tc_inner = false;
   ~CgWork();
   int ensure(const Operator &op, int niter);
   int ensure_scratch(size_t bytes);
@@ -140,6 +143,8 @@ int vec_convert(T *a, const S *b, long n, cudaStream_t s);
 // w = mask(QQ^T A_L u + 0.1 u)  (ax, cg.f:96-125), unfused path.
 template <typename T>
 int apply_ax(const Operator &op, T *w, const T *u, const T *g, cudaStream_t s);
+// the same in FP32 with the element products on the tensor cores (nb_ax_tc.cu)
+int apply_ax_tc(const Operator &op, float *w, const float *u, const float *g, cudaStream_t s);
 
 // CG of cg.f:2-84 on device data.  z may equal r (identity preconditioner).
 // precond: nullptr for the identity (hsmg_dum.f), else z = M^-1 r.
