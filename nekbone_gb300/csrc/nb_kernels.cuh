@@ -12,6 +12,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace nb {
 
 // ----------------------------------------------------------- arithmetic --
@@ -496,13 +498,50 @@ __global__ void __launch_bounds__(256)
   const T alpha = T(sc->alpha);
   const T alphm = -alpha;
   T part = T(0);
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
-       q += long(gridDim.x) * blockDim.x) {
-    x[q] = fma_rn(alpha, p[q], x[q]);
-    const T rv = fma_rn(alphm, w[q], r[q]);
-    r[q] = rv;
-    if (r32) r32[q] = float(rv);  // the FP32 V-cycle's input, as k_to_f32 makes it
-    part = fma_rn(mul_rn(rv, c[q]), rv, part);
+  // 16-byte loads and stores (two doubles or four floats a thread) when
+  // every vector allows them
+  constexpr int VEC = 16 / int(sizeof(T));
+  typedef typename std::conditional<sizeof(T) == 8, double2, float4>::type V;
+  const uintptr_t al = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
+                       reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(w) |
+                       reinterpret_cast<uintptr_t>(c);
+  const bool vec = (al & 15u) == 0 && n % VEC == 0 &&
+                   (!r32 || (reinterpret_cast<uintptr_t>(r32) & uintptr_t(4 * VEC - 1)) == 0);
+  if (vec) {
+    for (long v = long(blockIdx.x) * blockDim.x + threadIdx.x; v < n / VEC;
+         v += long(gridDim.x) * blockDim.x) {
+      alignas(16) T xa[VEC], ra[VEC], pa[VEC], wa[VEC], ca[VEC];
+      *reinterpret_cast<V *>(xa) = reinterpret_cast<const V *>(x)[v];
+      *reinterpret_cast<V *>(ra) = reinterpret_cast<const V *>(r)[v];
+      *reinterpret_cast<V *>(pa) = reinterpret_cast<const V *>(p)[v];
+      *reinterpret_cast<V *>(wa) = reinterpret_cast<const V *>(w)[v];
+      *reinterpret_cast<V *>(ca) = reinterpret_cast<const V *>(c)[v];
+      alignas(16) float r3[VEC];
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) {
+        xa[q] = fma_rn(alpha, pa[q], xa[q]);
+        ra[q] = fma_rn(alphm, wa[q], ra[q]);
+        r3[q] = float(ra[q]);
+        part = fma_rn(mul_rn(ra[q], ca[q]), ra[q], part);
+      }
+      reinterpret_cast<V *>(x)[v] = *reinterpret_cast<const V *>(xa);
+      reinterpret_cast<V *>(r)[v] = *reinterpret_cast<const V *>(ra);
+      if (r32) {
+        if constexpr (VEC == 2)
+          reinterpret_cast<float2 *>(r32)[v] = *reinterpret_cast<const float2 *>(r3);
+        else
+          reinterpret_cast<float4 *>(r32)[v] = *reinterpret_cast<const float4 *>(r3);
+      }
+    }
+  } else {
+    for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+         q += long(gridDim.x) * blockDim.x) {
+      x[q] = fma_rn(alpha, p[q], x[q]);
+      const T rv = fma_rn(alphm, w[q], r[q]);
+      r[q] = rv;
+      if (r32) r32[q] = float(rv);  // the FP32 V-cycle's input, as k_to_f32 makes it
+      part = fma_rn(mul_rn(rv, c[q]), rv, part);
+    }
   }
   const double s = block_sum<T>(part, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
