@@ -178,13 +178,42 @@ __global__ void __launch_bounds__(kThreads)
   const float alphm = -alpha;
   const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
   float part = 0.f;
+  const uintptr_t al = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
+                       reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(w) |
+                       reinterpret_cast<uintptr_t>(c);
+  if ((al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
+    // 16-byte accesses: chunk bounds are multiples of 4 (every lx1^3 of an
+    // even lx1 is)
+    for (long v = q0 / 4 + threadIdx.x; v < q1 / 4; v += kThreads) {
+      const float4 pv = reinterpret_cast<const float4 *>(p)[v];
+      const float4 wv = reinterpret_cast<const float4 *>(w)[v];
+      float4 rv = reinterpret_cast<const float4 *>(r)[v];
+      float4 xv = reinterpret_cast<const float4 *>(x)[v];
+      const float4 cv = reinterpret_cast<const float4 *>(c)[v];
+      xv.x = fma_rn(alpha, pv.x, xv.x);
+      xv.y = fma_rn(alpha, pv.y, xv.y);
+      xv.z = fma_rn(alpha, pv.z, xv.z);
+      xv.w = fma_rn(alpha, pv.w, xv.w);
+      rv.x = fma_rn(alphm, wv.x, rv.x);
+      rv.y = fma_rn(alphm, wv.y, rv.y);
+      rv.z = fma_rn(alphm, wv.z, rv.z);
+      rv.w = fma_rn(alphm, wv.w, rv.w);
+      reinterpret_cast<float4 *>(x)[v] = xv;
+      reinterpret_cast<float4 *>(r)[v] = rv;
+      part = fma_rn(mul_rn(rv.x, cv.x), rv.x, part);
+      part = fma_rn(mul_rn(rv.y, cv.y), rv.y, part);
+      part = fma_rn(mul_rn(rv.z, cv.z), rv.z, part);
+      part = fma_rn(mul_rn(rv.w, cv.w), rv.w, part);
+    }
+  } else {
 #pragma unroll 4
-  for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
-    const float pv = p[q], wv = w[q], rv0 = r[q], xv = x[q], cv = c[q];
-    x[q] = fma_rn(alpha, pv, xv);
-    const float rv = fma_rn(alphm, wv, rv0);
-    r[q] = rv;
-    part = fma_rn(mul_rn(rv, cv), rv, part);
+    for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
+      const float pv = p[q], wv = w[q], rv0 = r[q], xv = x[q], cv = c[q];
+      x[q] = fma_rn(alpha, pv, xv);
+      const float rv = fma_rn(alphm, wv, rv0);
+      r[q] = rv;
+      part = fma_rn(mul_rn(rv, cv), rv, part);
+    }
   }
   const double s = block_sum<float>(part, red);
   if (threadIdx.x == 0) part_pt[ch] = s;

@@ -584,16 +584,45 @@ __global__ void __launch_bounds__(256)
             T *mout = nullptr) {
   __shared__ double red[32];
   T part = T(0);
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
-       q += long(gridDim.x) * blockDim.x) {
-    T mv;
-    if (mf) {
-      mv = T(mf[q]);
-      mout[q] = mv;
-    } else {
-      mv = m[q];
+  // 16-byte accesses (two doubles or four floats a thread) when every vector
+  // allows them
+  constexpr int VEC = 16 / int(sizeof(T));
+  typedef typename std::conditional<sizeof(T) == 8, double2, float4>::type V;
+  typedef typename std::conditional<sizeof(T) == 8, float2, float4>::type VF;
+  const uintptr_t al = reinterpret_cast<uintptr_t>(a) | reinterpret_cast<uintptr_t>(b) |
+                       reinterpret_cast<uintptr_t>(mf ? mout : m);
+  const bool vec = (al & 15u) == 0 && n % VEC == 0 &&
+                   (!mf || (reinterpret_cast<uintptr_t>(mf) & uintptr_t(4 * VEC - 1)) == 0);
+  if (vec) {
+    for (long v = long(blockIdx.x) * blockDim.x + threadIdx.x; v < n / VEC;
+         v += long(gridDim.x) * blockDim.x) {
+      alignas(16) T aa[VEC], ba[VEC], ma[VEC];
+      *reinterpret_cast<V *>(aa) = reinterpret_cast<const V *>(a)[v];
+      *reinterpret_cast<V *>(ba) = reinterpret_cast<const V *>(b)[v];
+      if (mf) {
+        alignas(16) float fa[VEC];
+        *reinterpret_cast<VF *>(fa) = reinterpret_cast<const VF *>(mf)[v];
+#pragma unroll
+        for (int q = 0; q < VEC; ++q) ma[q] = T(fa[q]);
+        reinterpret_cast<V *>(mout)[v] = *reinterpret_cast<const V *>(ma);
+      } else {
+        *reinterpret_cast<V *>(ma) = reinterpret_cast<const V *>(m)[v];
+      }
+#pragma unroll
+      for (int q = 0; q < VEC; ++q) part = fma_rn(mul_rn(aa[q], ba[q]), ma[q], part);
     }
-    part = fma_rn(mul_rn(a[q], b[q]), mv, part);
+  } else {
+    for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
+         q += long(gridDim.x) * blockDim.x) {
+      T mv;
+      if (mf) {
+        mv = T(mf[q]);
+        mout[q] = mv;
+      } else {
+        mv = m[q];
+      }
+      part = fma_rn(mul_rn(a[q], b[q]), mv, part);
+    }
   }
   const double s = block_sum<T>(part, red);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
