@@ -219,6 +219,51 @@ def test_cg_seeded_rhs_device_api(nb):
     assert rel(vs2[0].cpu().numpy(), o["x"]) < 1e-12
 
 
+def test_cg_device_api_unaligned_vectors(nb):
+    """Vectors one element off 16-byte alignment take the update's and
+    glsc3's 8-byte (FP64) / 4-byte (FP32) paths: the same iterates as the
+    aligned vectors' 16-byte paths, to rounding."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(3, 4, 3, 8, mask_mode=1)
+    ctx = O.Ctx(3, 4, 3, 8, mask_mode=1)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n + 1, dtype=torch.float64, device=dev)
+    f = torch.empty(n + 1, dtype=torch.float64, device=dev)
+    m.setup_g(g.data_ptr())
+    m.set_multiplicity(c[1:].data_ptr())
+    m.rhs_uniform(f[1:].data_ptr(), c[1:].data_ptr(), 77)
+    xs = []
+    for off in (0, 1):
+        fo = f[1:].clone() if off == 0 else f[1:]
+        co = c[1:].clone() if off == 0 else c[1:]
+        vs = [torch.zeros(n + 1, dtype=torch.float64, device=dev)[off:off + n] for _ in range(5)]
+        assert (vs[0].data_ptr() % 16 == 0) == (off == 0)
+        m.cg(*(t.data_ptr() for t in (vs[0], fo, g, co, vs[1], vs[2], vs[3], vs[4])), 60)
+        xs.append(vs[0].cpu().numpy())
+    o = ctx.cg(f[1:].cpu().numpy(), g.cpu().numpy(), c[1:].cpu().numpy(), 60)
+    for x in xs:
+        assert rel(x, o["x"]) < 1e-12
+    assert rel(xs[0], xs[1]) < 1e-13
+    # FP32 CG on unaligned vectors follows the aligned one to FP32 rounding
+    f32, g32, c32 = f[1:].float(), g.float(), c[1:].float()
+    hs = []
+    for off in (0, 1):
+        fo = f32.clone() if off == 0 else torch.zeros(n + 1, dtype=torch.float32, device=dev)
+        if off == 1:
+            fo[1:] = f32
+            fo = fo[1:]
+        co = c32.clone() if off == 0 else torch.zeros(n + 1, dtype=torch.float32, device=dev)
+        if off == 1:
+            co[1:] = c32
+            co = co[1:]
+        v = [torch.zeros(n + 1, dtype=torch.float32, device=dev)[off:off + n] for _ in range(4)]
+        hs.append(m.cg_f32(v[0].data_ptr(), fo.data_ptr(), g32.data_ptr(), co.data_ptr(),
+                           v[1].data_ptr(), v[2].data_ptr(), v[3].data_ptr(), 20, hist=True))
+    assert np.allclose(hs[0][:, 0], hs[1][:, 0], rtol=1e-4)
+
+
 def test_fp32_and_mixed_precision(nb):
     torch = pytest.importorskip("torch")
     m = nb.DeviceMesh(4, 4, 4, 8, mask_mode=1)
