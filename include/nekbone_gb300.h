@@ -296,6 +296,13 @@ int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
  * the exact product; *mismatches = number of wrong results (0 = pass). */
 int nb_tc_selftest(int bf16, int *mismatches);
 
+/* Self-test of the bounded waits: one warp waits on an mbarrier that nothing
+ * arrives on, giving up after `polls` polls (1..65536) as every wait in the
+ * library's kernels gives up after its limit.  Returns the status such a
+ * timeout produces (NB_ERR_CUDA, "a device-side wait timed out") and clears
+ * the device error word, so the next call runs normally. */
+int nb_wait_selftest(unsigned polls);
+
 /* Synchronise the library's stream. */
 int nb_sync(void);
 /* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for

@@ -56,6 +56,7 @@ EXPORTS = (
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
+    "nb_wait_selftest",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -127,6 +128,8 @@ lib.nb_set_shared_metric.restype = None
 lib.nb_set_shared_metric.argtypes = [_i]
 lib.nb_set_mixed_tensor_cores.restype = None
 lib.nb_set_mixed_tensor_cores.argtypes = [_i]
+lib.nb_wait_selftest.restype = _i
+lib.nb_wait_selftest.argtypes = [_C.c_uint]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
@@ -659,6 +662,12 @@ def tc_selftest(bf16: bool = False) -> int:
     bad = _C.c_int(-1)
     _check(lib.nb_tc_selftest(1 if bf16 else 0, _C.byref(bad)))
     return bad.value
+
+
+def wait_selftest(polls: int = 256) -> None:
+    """Runs a bounded wait that nothing completes; raises NekboneError with
+    the status a timed-out device wait produces."""
+    _check(lib.nb_wait_selftest(polls))
 
 
 def stream_handle() -> int:

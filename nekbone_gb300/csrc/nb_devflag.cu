@@ -2,6 +2,7 @@
 // waits (bulk copies, barriers) set a bit in it when a wait runs out instead
 // of hanging; the host checks it after solves.
 #include "nb_internal.h"
+#include "nb_tma.cuh"
 
 namespace nb {
 
@@ -35,3 +36,35 @@ int device_error_check(cudaStream_t s) {
 }
 
 }  // namespace nb
+
+namespace nb {
+cudaStream_t lib_stream();
+
+namespace {
+// One warp waits on an mbarrier that nothing arrives on, at most `polls`
+// polls a thread: the bounded wait gives up, sets the error word and the
+// kernel returns with nothing in flight.
+__global__ void k_wait_selftest(unsigned polls, unsigned *err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  mbar_wait_bounded(&bar, 0, err, polls);
+}
+}  // namespace
+}  // namespace nb
+
+// The path every bounded wait takes when it runs out: the kernel returns,
+// the host reads the error word and reports it, the context stays usable.
+extern "C" int nb_wait_selftest(unsigned polls) {
+  using namespace nb;
+  clear_status();
+  if (polls == 0 || polls > (1u << 16))
+    return fail(NB_ERR_ARG, "nb_wait_selftest: polls=%u (1..65536)", polls);
+  unsigned *err = device_error_word();
+  if (!err) return fail(NB_ERR_CUDA, "nb_wait_selftest: no device error word");
+  cudaStream_t s = lib_stream();
+  NB_CUDA(cudaStreamSynchronize(s));
+  k_wait_selftest<<<1, 32, 0, s>>>(polls, err);
+  NB_CUDA(cudaGetLastError());
+  return device_error_check(s);
+}

@@ -77,3 +77,18 @@ def test_pcg_needs_multigrid_and_batch_checks(nb):
     nb.sync()
     assert all(b.result(p)[2] <= 1e-10 for p in range(b.nprob))
     b.close()
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(nb):
+    """A device wait that nothing completes gives up after its poll limit:
+    the call reports the timeout through the device error word, and the
+    next calls on the same context run normally."""
+    with pytest.raises(nb.NekboneError) as ei:
+        nb.wait_selftest(256)
+    assert "timed out" in str(ei.value)
+    assert nb.tc_selftest() == 0
+    a = np.arange(1.0, 9.0)
+    assert nb.glsc3(a, a, np.ones(8)) == float((a * a).sum())
+    nb.sync()
+    with pytest.raises(nb.NekboneError):
+        nb.wait_selftest(0)
