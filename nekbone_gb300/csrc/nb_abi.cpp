@@ -628,10 +628,12 @@ void cg_(double *x, const double *f, const double *g, const double *c,
   if (cg_device(*op, S.wk, dx, df, dg, dc, dr, dw, dp, dz, *niter, M.get(),
                 false, S.s))
     return;
-  if (d2h(x, dx, nn * 8) || d2h(r, dr, nn * 8) || d2h(w, dw, nn * 8) ||
-      d2h(p, dp, nn * 8))
+  if (d2h(x, dx, nn * 8) || d2h(r, dr, nn * 8)) return;
+  // w, p and z are written only by an iteration (cg.f:48-75); with niter = 0
+  // the caller's arrays stay as they were, as in the reference
+  if (*niter > 0 &&
+      (d2h(w, dw, nn * 8) || d2h(p, dp, nn * 8) || d2h(z, dz, nn * 8)))
     return;
-  if (*niter > 0 && d2h(z, dz, nn * 8)) return;
   if (sync() || device_error_check(S.s)) return;
   const int iter = *niter + 1;
   for (int k = 0; k < *niter; ++k) S.flop_a += ax_flops(S.nx1, S.nelt);

@@ -192,6 +192,33 @@ def test_cg_c1_matches_oracle(nb, mask_mode):
     assert fc == 101 * 15 * mesh.n
 
 
+@pytest.mark.parametrize("mask_mode", [0, 1])
+@pytest.mark.parametrize("niter", [0, 1, 2])
+def test_cg_few_iterations_match_oracle(nb, mask_mode, niter):
+    """The drop-in cg with 0, 1 and 2 iterations: x, r, w, p (and z once an
+    iteration ran) and the flop count (the reference counts niter + 1
+    iterations, cg.f:81) as the oracle gives them."""
+    mesh = nb.Nekbone(2, 3, 2, 6, mask_mode=mask_mode)
+    ctx = O.Ctx(2, 3, 2, 6, mask_mode=mask_mode)
+    c = mesh.set_multiplicity()
+    g = mesh.setup_g()
+    f = mesh.set_f(c)
+    mesh.mask_reset()
+    nb.Nekbone.set_flops(0.0, 0.0)
+    work = tuple(np.zeros(mesh.n) for _ in range(5))
+    owork = tuple(np.zeros(mesh.n) for _ in range(5))
+    x, r, w, p, z, fc = mesh.cg(f, g, c, niter, 0.0, work)
+    o = ctx.cg(f, g, c, niter, work=owork)
+    scale = np.max(np.abs(f))
+    assert np.max(np.abs(x - o["x"])) <= 1e-13 * max(np.max(np.abs(o["x"])), scale)
+    pairs = [("r", r, o["r"]), ("w", w, o["w"]), ("p", p, o["p"])]
+    if niter > 0:
+        pairs.append(("z", z, o["z"]))
+    for name, a, b in pairs:
+        assert np.max(np.abs(a - b)) <= 1e-13 * scale, name
+    assert fc == (niter + 1) * 15 * mesh.n
+
+
 def test_cg_seeded_rhs_device_api(nb):
     torch = pytest.importorskip("torch")
     m = nb.DeviceMesh(4, 4, 4, 10, mask_mode=1)
