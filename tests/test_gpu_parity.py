@@ -219,6 +219,30 @@ def test_cg_few_iterations_match_oracle(nb, mask_mode, niter):
     assert fc == (niter + 1) * 15 * mesh.n
 
 
+@pytest.mark.parametrize("mask_mode", [0, 1])
+@pytest.mark.parametrize("dims", [(1, 1, 1, 5), (2, 1, 1, 4), (1, 1, 3, 6)])
+def test_cg_smallest_meshes_match_oracle(nb, mask_mode, dims):
+    """One element, and a row of two or three: the boundary groups are all
+    pairs or singletons (the domain faces), and the drop-in cg still matches
+    the oracle."""
+    mesh = nb.Nekbone(*dims, mask_mode=mask_mode)
+    ctx = O.Ctx(*dims, mask_mode=mask_mode)
+    c = mesh.set_multiplicity()
+    g = mesh.setup_g()
+    f = mesh.set_f(c)
+    assert np.array_equal(c, ctx.set_multiplicity())
+    mesh.mask_reset()
+    work = tuple(np.zeros(mesh.n) for _ in range(5))
+    owork = tuple(np.zeros(mesh.n) for _ in range(5))
+    for call in range(2):
+        x, r, w, p, z, fc = mesh.cg(f, g, c, 10, 0.0, work)
+        o = ctx.cg(f, g, c, 10, work=owork)
+        scale = np.max(np.abs(f))
+        assert np.max(np.abs(x - o["x"])) <= 1e-12 * max(np.max(np.abs(o["x"])), scale), call
+        for name, a, b in (("r", r, o["r"]), ("w", w, o["w"]), ("p", p, o["p"])):
+            assert np.max(np.abs(a - b)) <= 1e-12 * scale, (call, name)
+
+
 def test_cg_seeded_rhs_device_api(nb):
     torch = pytest.importorskip("torch")
     m = nb.DeviceMesh(4, 4, 4, 10, mask_mode=1)
