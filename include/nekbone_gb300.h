@@ -303,6 +303,21 @@ int nb_tc_selftest(int bf16, int *mismatches);
  * the device error word, so the next call runs normally. */
 int nb_wait_selftest(unsigned polls);
 
+/* Timeout self-test inside the real kernels: while on (on != 0), every
+ * element kernel that brings its metric block in by a bulk copy (the FP32
+ * operators with per-element metrics, the batched FP32 operator) sets its
+ * barrier to expect 16 bytes more than the copy brings, so its bounded wait
+ * runs out for certain.  The CTA then lets the copy land, skips the
+ * element's arithmetic and stores, and sets the device error word.  Takes
+ * effect for launches enqueued (and batch graphs built) after the call.
+ * Results computed meanwhile are invalid; the synchronising calls report
+ * NB_ERR_CUDA ("a device-side wait timed out") once and clear the word.
+ * Timeouts are reported by nb_sync, cg_, nb_cg_tol, nb_cg_mixed, nb_pcg_tol,
+ * nb_batch_result and nb_batch_cycles; the asynchronous calls (nb_ax,
+ * nb_ax_f32, nb_ax_tc, nb_cg, nb_batch_solve) leave them to the next of
+ * those.  No counterpart in the reference. */
+int nb_set_wait_test(int on);
+
 /* Synchronise the library's stream. */
 int nb_sync(void);
 /* The CUDA stream (cudaStream_t) every nb_* and drop-in call runs on, for

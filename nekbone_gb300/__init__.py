@@ -56,7 +56,7 @@ EXPORTS = (
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
-    "nb_wait_selftest",
+    "nb_wait_selftest", "nb_set_wait_test",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -130,6 +130,8 @@ lib.nb_set_mixed_tensor_cores.restype = None
 lib.nb_set_mixed_tensor_cores.argtypes = [_i]
 lib.nb_wait_selftest.restype = _i
 lib.nb_wait_selftest.argtypes = [_C.c_uint]
+lib.nb_set_wait_test.restype = _i
+lib.nb_set_wait_test.argtypes = [_i]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
@@ -668,6 +670,12 @@ def wait_selftest(polls: int = 256) -> None:
     """Runs a bounded wait that nothing completes; raises NekboneError with
     the status a timed-out device wait produces."""
     _check(lib.nb_wait_selftest(polls))
+
+
+def set_wait_test(on: bool) -> None:
+    """Makes the bulk-copy waits of later launches run out on purpose (the
+    timeout path of the real kernels); off restores normal runs."""
+    _check(lib.nb_set_wait_test(1 if on else 0))
 
 
 def stream_handle() -> int:

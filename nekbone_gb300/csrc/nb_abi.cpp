@@ -1084,6 +1084,7 @@ int nb_pcg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
     if (rn0 > 0 && rn / rn0 <= tol) break;
   }
   if (stt) return stt;
+  NB_TRY(device_error_check(s));
   if (iters) *iters = done;
   if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
   return NB_OK;

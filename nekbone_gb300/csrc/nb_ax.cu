@@ -19,6 +19,7 @@ template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
+  a.wait_test = wait_test_mode();
   if (op.order == 1 && op.eo_ok) {  // even-odd split (FP64 pipe bound)
     if (mode == 0) return launch_ax_eo_m0(op.lx, a, op.EO.data(), s);
     if (mode == 1) return launch_ax_eo_m1(op.lx, a, op.EO.data(), s);
@@ -33,6 +34,7 @@ template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
   a.nelt = op.nelt;
   a.err = device_error_word();
+  a.wait_test = wait_test_mode();
   if (op.order == 1 && op.eo_ok && mode != 2) {  // even-odd, one line per thread
     if (mode == 0) return launch_ax_eo32_m0(op.lx, a, op.EO.data(), s);
     return launch_ax_eo32_m1(op.lx, a, op.EO.data(), s);

@@ -498,7 +498,7 @@ struct Batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   double g_tol = -1.0, g_itol = -1.0;
-  int g_inner = -1, g_outer = -1;
+  int g_inner = -1, g_outer = -1, g_wtest = -1;
   double itol = 0.0;  // 0: every cycle runs inner iterations; > 0: per-problem stop
 
   ~Batch() {
@@ -533,6 +533,8 @@ struct Batch {
       a.el0 = G.el0;
       a.nel = G.nel;
       a.first = it == 1;
+      a.err = device_error_word();
+      a.wait_test = wait_test_mode();
       NB_TRY(batch_ax_f32(G.lx, G.tune.epb32, G.tune.rd32, a, s));
     }
     return NB_OK;
@@ -555,6 +557,8 @@ struct Batch {
       a.pt0 = G.pt0;
       a.el0 = G.el0;
       a.nel = G.nel;
+      a.err = device_error_word();
+      a.wait_test = wait_test_mode();
       NB_TRY(batch_ax_f64(G.lx, G.tune.epb64, a, s));
     }
     return NB_OK;
@@ -600,7 +604,8 @@ struct Batch {
   }
 
   int build_graph(double tol, int inner, int max_outer) {
-    if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer && itol == g_itol)
+    if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer && itol == g_itol &&
+        wait_test_mode() == g_wtest)
       return NB_OK;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -667,6 +672,7 @@ struct Batch {
     g_inner = inner;
     g_outer = max_outer;
     g_itol = itol;
+    g_wtest = wait_test_mode();
     return NB_OK;
   }
 };
@@ -1038,6 +1044,8 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.el0 = G.el0;
       a.nel = G.nel;
       a.first = 0;
+      a.err = device_error_word();
+      a.wait_test = wait_test_mode();
       st = Batch::batch_ax_f32(G.lx, sh.first, sh.second, a, s);
       if (st) break;
       cudaEventRecord(e0, s);
@@ -1073,6 +1081,8 @@ int nb_batch_tune(nb_batch *b, int reps) {
       a.pt0 = G.pt0;
       a.el0 = G.el0;
       a.nel = G.nel;
+      a.err = device_error_word();
+      a.wait_test = wait_test_mode();
       st = Batch::batch_ax_f64(G.lx, epb, a, s);
       if (st) break;
       cudaEventRecord(e0, s);
@@ -1132,7 +1142,7 @@ int nb_batch_result(const nb_batch *b, int prob, int *outer, int *inner, double 
   BatchScalars S;
   cudaStream_t s = lib_stream();
   NB_CUDA(cudaMemcpyAsync(&S, b->B.sc + b->B.slot[prob], sizeof(S), cudaMemcpyDeviceToHost, s));
-  NB_CUDA(cudaStreamSynchronize(s));
+  NB_TRY(device_error_check(s));
   if (outer) *outer = S.outer;
   if (inner) *inner = S.inner;
   if (relres) *relres = S.rn0 > 0 ? S.rn / S.rn0 : 0.0;
@@ -1145,7 +1155,7 @@ int nb_batch_cycles(const nb_batch *b, int *cycles) {
   int v = 0;
   cudaStream_t s = lib_stream();
   NB_CUDA(cudaMemcpyAsync(&v, b->B.cycles, sizeof(int), cudaMemcpyDeviceToHost, s));
-  NB_CUDA(cudaStreamSynchronize(s));
+  NB_TRY(device_error_check(s));
   if (cycles) *cycles = v;
   return NB_OK;
 }

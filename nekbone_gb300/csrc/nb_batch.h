@@ -66,6 +66,8 @@ struct BaxArgs {
   long pt0;            // first point of this lx1 group
   int el0, nel;        // element range of this lx1 group
   int first;           // MODE 1: first inner iteration
+  unsigned *err;       // device error word (bounded waits on the metric copy)
+  int wait_test;       // timeout self-test of that wait (block_copy_begin)
 };
 
 // The batched element operator for one lx1 (T float: MODE 1, T double:

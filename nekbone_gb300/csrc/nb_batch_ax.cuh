@@ -248,12 +248,8 @@ __global__ void __launch_bounds__(LX * LX)
   const int prob = a.el_prob[e];
   if (!a.sc[prob].active || (MODE == 1 && !a.sc[prob].iactive)) return;  // one element
   const size_t base = size_t(a.pt0) + size_t(blockIdx.x) * L3;
-  if (TMAG && t == 0) {
-    constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));
-    mbar_init(&sm.bar, 1);
-    mbar_arrive_expect_tx(&sm.bar, GBYTES);
-    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
-  }
+  if (TMAG && t == 0)
+    block_copy_begin(&sm.bar, sm.g, a.g + 6 * base, unsigned(6 * L3 * sizeof(T)), a.wait_test);
   // coefficients as in k_ax_eo: FP32 from the parameter bank, FP64 staged
   // in shared memory
   constexpr bool CPAR = sizeof(T) == 4 && LX <= 12;
@@ -319,7 +315,7 @@ __global__ void __launch_bounds__(LX * LX)
   T wtreg[LX];
   eo_line<T, LX>(ureg, Ed, Od, wtreg);
   __syncthreads();
-  if (TMAG) mbar_wait_bounded(&sm.bar, 0, nullptr);
+  if (TMAG && !block_copy_wait(&sm.bar, a.err, a.wait_test, sm.red, a.g + 6 * base)) return;
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = eo_at<T, LX>(i, j, k);

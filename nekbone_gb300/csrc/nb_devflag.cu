@@ -8,7 +8,10 @@ namespace nb {
 
 namespace {
 unsigned *g_err = nullptr;
+int g_wait_test = 0;
 }
+
+int wait_test_mode() { return g_wait_test; }
 
 unsigned *device_error_word() {
   if (!g_err) {
@@ -67,4 +70,14 @@ extern "C" int nb_wait_selftest(unsigned polls) {
   k_wait_selftest<<<1, 32, 0, s>>>(polls, err);
   NB_CUDA(cudaGetLastError());
   return device_error_check(s);
+}
+
+// The same path in the real kernels: while on, every element kernel that
+// brings its metric block in by a bulk copy sets its barrier to expect 16
+// more bytes than the copy brings, so its bounded wait runs out; the CTA
+// then lets the copy land, skips the element and sets the error word.
+extern "C" int nb_set_wait_test(int on) {
+  nb::clear_status();
+  nb::g_wait_test = on != 0;
+  return nb::NB_OK;
 }

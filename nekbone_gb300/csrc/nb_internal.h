@@ -57,6 +57,9 @@ void set_error_mode(int mode);
 // check, which synchronises the stream and fails if a wait ran out.
 unsigned *device_error_word();
 int device_error_check(cudaStream_t s);
+// Whether launches enqueued now run the bulk-copy timeout self-test
+// (nb_set_wait_test): their metric-copy waits run out on purpose.
+int wait_test_mode();
 
 constexpr int kMaxLx = 16;     // largest lx1 with a specialised ax kernel
 constexpr int kMaxNl = 24;     // largest 1-D size of a multigrid tensor apply

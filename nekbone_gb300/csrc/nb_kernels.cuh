@@ -120,6 +120,7 @@ struct AxArgs {
   double scale;      // MODE 2: its scale
   unsigned *err;     // device error word for bounded waits (may be null)
   int g_uniform;     // every element's metric block equals element 0's: read that one
+  int wait_test;     // timeout self-test of the bulk-copy wait (block_copy_begin)
 };
 
 template <typename T, int LX>
@@ -671,7 +672,7 @@ struct AxTmaShared {
   alignas(16) float Dr[LX * LX];
   alignas(16) float Dc[LX * LX];
   alignas(8) uint64_t bar;
-  double red[32];
+  alignas(16) double red[32];
 };
 
 template <int LX, int MODE>
@@ -686,11 +687,7 @@ __global__ void __launch_bounds__(LX * LX)
   const int e = blockIdx.x;
   const size_t base = size_t(e) * L3;
 
-  if (tid == 0) {
-    mbar_init(&sm.bar, 1);
-    mbar_arrive_expect_tx(&sm.bar, GBYTES);
-    bulk_g2s(sm.g, a.g + 6 * base, GBYTES, &sm.bar);
-  }
+  if (tid == 0) block_copy_begin(&sm.bar, sm.g, a.g + 6 * base, GBYTES, a.wait_test);
   {
     const int r = tid % LX, m = tid / LX;
     const float d = a.D[r + m * LX];
@@ -729,7 +726,7 @@ __global__ void __launch_bounds__(LX * LX)
     Di[m] = sm.Dr[i * LX + m];
     Dj[m] = sm.Dr[j * LX + m];
   }
-  mbar_wait_bounded(&sm.bar, 0, a.err);
+  if (!block_copy_wait(&sm.bar, a.err, a.wait_test, sm.red, a.g)) return;
 
   float wtreg[LX];
 #pragma unroll
@@ -853,7 +850,7 @@ struct AxEoShared {
   T C[N];
   T E4[4 * (LX / 2) * (LX / 2)];  // E, O of D, then E, O of D^T
   alignas(8) uint64_t bar;
-  double red[32];
+  alignas(16) double red[32];
 };
 
 
@@ -947,12 +944,8 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
   const size_t base = size_t(e) * L3;
   // the element's metric block (the shared one when all blocks are equal)
   const T *gblk = a.g + (a.g_uniform ? size_t(0) : 6 * base);
-  if (TMAG && t == 0) {
-    constexpr unsigned GBYTES = unsigned(6 * L3 * sizeof(T));
-    mbar_init(&sm.bar, 1);
-    mbar_arrive_expect_tx(&sm.bar, GBYTES);
-    bulk_g2s(sm.g, gblk, GBYTES, &sm.bar);
-  }
+  if (TMAG && t == 0)
+    block_copy_begin(&sm.bar, sm.g, gblk, unsigned(6 * L3 * sizeof(T)), a.wait_test);
   // FP32 up to lx1 = 12 reads the coefficients from the parameter bank.
   // FP64 and the larger FP32 shapes copy them to shared memory: from the
   // parameter bank the compiler keeps many of them in registers, and those
@@ -1027,7 +1020,7 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
   __syncthreads();
 
   // metric, cg.f:156-163 (wr, ws back into B, C; wt in registers)
-  if (TMAG) mbar_wait_bounded(&sm.bar, 0, a.err);
+  if (TMAG && !block_copy_wait(&sm.bar, a.err, a.wait_test, sm.red, gblk)) return;
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = eo_at<T, LX>(i, j, k);

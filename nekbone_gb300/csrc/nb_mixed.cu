@@ -176,6 +176,7 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
     }
   }
   if (st) return st;
+  NB_TRY(device_error_check(s));
   if (iters) *iters = done;
   if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;
   return NB_OK;
@@ -301,6 +302,7 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     ++k;
   }
   if (st) return st;
+  NB_TRY(device_error_check(s));
   if (outer) *outer = k;
   if (inner_total) *inner_total = inner;
   if (relres) *relres = rn0 > 0 ? rn / rn0 : 0.0;

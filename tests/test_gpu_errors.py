@@ -92,3 +92,54 @@ def test_bounded_wait_times_out_and_context_stays_usable(nb):
     nb.sync()
     with pytest.raises(nb.NekboneError):
         nb.wait_selftest(0)
+
+
+def test_batched_metric_copy_timeout_is_reported(nb):
+    """The batched FP32 operator brings each element's metric block in by a
+    bulk copy.  With the wait self-test on, that wait runs out in every
+    element: the solve's results are flagged (NB_ERR_CUDA from
+    nb_batch_result) instead of being returned as valid, and after the
+    switch is off a rebuilt solve is correct again on the same context."""
+    probs = [(2, 2, 2, 6), (1, 1, 2, 8)]
+    nb.set_wait_test(True)
+    try:
+        b = nb.Batch(probs)
+        b.setup(5)
+        b.solve(1e-10, 20, 5)
+        with pytest.raises(nb.NekboneError) as ei:
+            b.result(0)
+        assert "timed out" in str(ei.value)
+    finally:
+        nb.set_wait_test(False)
+    b.solve(1e-10, 20, 20)
+    assert all(b.result(p)[2] <= 1e-10 for p in range(b.nprob))
+    b.close()
+
+
+def test_operator_metric_copy_timeout_is_reported(nb):
+    """The same for the single-mesh FP32 operator with a per-element (here
+    deformed) metric: nb_ax_f32 is asynchronous, so nb_sync reports the
+    timeout; with the switch off the same call matches the FP64 operator."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(2, 2, 2, 8, mask_mode=1)
+    n = m.n
+    g = torch.zeros(6 * n, dtype=torch.float64, device="cuda")
+    m.setup_g_deformed(g.data_ptr(), 3, 0.1)
+    u = torch.rand(n, dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(1))
+    g32, u32 = g.float(), u.float()
+    w32 = torch.zeros(n, dtype=torch.float32, device="cuda")
+    nb.set_wait_test(True)
+    try:
+        m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())
+        with pytest.raises(nb.NekboneError) as ei:
+            nb.sync()
+        assert "timed out" in str(ei.value)
+    finally:
+        nb.set_wait_test(False)
+    m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())
+    w = torch.zeros(n, dtype=torch.float64, device="cuda")
+    m.ax(w.data_ptr(), u.data_ptr(), g.data_ptr())
+    nb.sync()
+    err = float((w32.double() - w).abs().max() / w.abs().max())
+    assert err < 1e-5
+    m.close()
