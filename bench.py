@@ -16,12 +16,17 @@ reference's DOF convention, n = nelt*lx1^3).
   roofline -- the dominant kernel (the fused element operator k_ax), from its
             own CUDA-event time over a timed CG iteration loop.
   mixed  -- time to relative residual 1e-10 of plain FP64 CG and of the
-            mixed-precision solver (FP32 inner CG in FP64 defect correction).
+            mixed-precision solver (FP32 inner CG in FP64 defect correction),
+            each solution's true residual recomputed on the host by the
+            oracle's own ax (cpu_relres).
   cpu_baseline -- the oracle (CPU restatement, OpenMP over elements) on the
-            host cores, on a bounded sample of the same workload.
+            host cores, on a bounded sample of the same workload (the same
+            32^3 mesh, fewer iterations).
 
 --impl reference runs the reference's CPU algorithm (the oracle port; the
-Fortran reference has no compiler in this image) on the same configuration.
+Fortran reference has no compiler in this image) on the same configuration:
+the same 32^3 mesh and right-hand side, a bounded number of CG iterations
+per step (the metric is a per-iteration rate).
 """
 from __future__ import annotations
 
@@ -41,13 +46,14 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "GDOF·iter/s (lx1=12, 32^3 elems); mixed vs FP64 GPU time to rel. resid 1e-10"
-# FP64 FMA throughput of one GB300 (an FMA-chain probe: 1/72 of FP32)
-FP64_PEAK_TFLOPS = 1.055
-# DRAM read + write bytes per point of k_ax_eo4<double,12,1> (ncu, 16^3
-# elements: 531.7 MB + 120.9 MB over 7,077,888 points); the kernel streams,
-# so traffic scales with n
-DRAM_BYTES_PER_POINT_AX_EO = (531.699456e6 + 120.930048e6) / 7077888
 UNIT = "GDOF*iter/s"
+# DRAM read + write bytes per point of each FP64 element operator at lx1 = 12
+# from one ncu capture on 16^3 elements (7,077,888 points); the kernels
+# stream, so traffic scales with n.  Source: the profiles/ summaries named.
+DRAM_BYTES_PER_POINT = {
+    1: ((531.699456e6 + 120.930048e6) / 7077888, "profiles/k_ax_eo_fp64_lx12_16cubed.md"),
+}
+RHS_SEED = 20260
 
 
 def parse():
@@ -64,8 +70,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--tol", type=float, default=1e-10)
-    ap.add_argument("--cpu-sample-nel", type=int, default=16)
-    ap.add_argument("--cpu-sample-iters", type=int, default=250)
+    ap.add_argument("--order", type=int, default=2, choices=[0, 1, 2],
+                    help="FP64 operator form: 0 the reference's summation order, 1 even-odd "
+                         "on the FP64 pipe, 2 even-odd in 64-bit fixed point on the integer "
+                         "pipes")
+    ap.add_argument("--cpu-sample-iters", type=int, default=8,
+                    help="CG iterations per CPU sample of the 32^3 workload")
     ap.add_argument("--case", choices=["cg", "tc", "batch", "hsmg", "mixed"], default="cg",
                     help="cg: the benchmark; tc / batch / hsmg / mixed: a small case of the "
                          "tensor-core operator / the batched solver / hsmg PCG / the mixed "
@@ -135,20 +145,64 @@ class Clocks:
 
 
 # ------------------------------------------------------------- CPU oracle --
-def cpu_rate(nel: int, lx: int, iters: int, threads: int):
-    """GDOF*iter/s of the oracle's cg (OpenMP over elements) on nel^3 x lx."""
-    sys.path.insert(0, str(ROOT / "tests"))
-    import oracle_lib as O
-    ctx = O.Ctx(nel, nel, nel, lx, mask_mode=1, nthreads=threads, fma=False)
-    g = ctx.setup_g()
-    c = ctx.set_multiplicity()
-    f = ctx.set_f(c)
-    ctx.maskit(f)
-    work = tuple(np.zeros(ctx.n) for _ in range(5))
-    t0 = time.perf_counter()
-    ctx.cg(f, g, c, iters, work=work)
-    dt = time.perf_counter() - t0
-    return ctx.n * iters / dt / 1e9, dt, ctx.n
+def uniform_pm1(seed: int, ids: np.ndarray) -> np.ndarray:
+    """The library's counter-based uniform [-1, 1) of (seed, global id)
+    (splitmix64 finaliser), restated in numpy for the CPU side."""
+    z = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + ids.astype(np.uint64)
+         + np.uint64(0x632BE59BD9B4E019))
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (2.0 / 9007199254740992.0) - 1.0
+
+
+def global_ids(nel: int, lx: int) -> np.ndarray:
+    """set_vert_box's global numbering (prox_dssum.f:42-73) of a nel^3 brick,
+    in the local point order (element ex fastest, then i, j, k)."""
+    nn = lx - 1
+    ax = nn * nel + 1
+    e = np.arange(nel, dtype=np.int64)
+    q = np.arange(lx, dtype=np.int64)
+    ez, ey, ex, k, j, i = np.ix_(e, e, e, q, q, q)
+    return (1 + (nn * ex + i) + (nn * ey + j) * ax + (nn * ez + k) * ax * ax).reshape(-1)
+
+
+class CpuCase:
+    """The oracle on the headline mesh with the headline inputs: setup_g's
+    metric, the inverse multiplicity and nb_rhs_uniform's right-hand side
+    (uniform per global point, dssum, times c, masked)."""
+
+    def __init__(self, nel: int, lx: int, threads: int, seed: int = RHS_SEED):
+        sys.path.insert(0, str(ROOT / "tests"))
+        import oracle_lib as O
+        t0 = time.perf_counter()
+        self.ctx = O.Ctx(nel, nel, nel, lx, mask_mode=1, nthreads=threads, fma=False)
+        self.g = self.ctx.setup_g()
+        self.c = self.ctx.set_multiplicity()
+        f = uniform_pm1(seed, global_ids(nel, lx))
+        self.ctx.dssum(f)
+        f *= self.c
+        self.ctx.maskit(f)
+        self.f = f
+        self.n = self.ctx.n
+        self.threads = threads
+        self.setup_s = time.perf_counter() - t0
+        self.work = tuple(np.zeros(self.n) for _ in range(5))
+
+    def cg(self, iters: int):
+        t0 = time.perf_counter()
+        o = self.ctx.cg(self.f, self.g, self.c, iters, work=self.work)
+        return o, time.perf_counter() - t0
+
+    def rate(self, iters: int):
+        _, dt = self.cg(iters)
+        return self.n * iters / dt / 1e9, dt
+
+    def relres(self, x: np.ndarray) -> float:
+        """sqrt(r'Cr) / sqrt(f'Cf), r = mask(f - A x), A the oracle's ax."""
+        r = self.f - self.ctx.ax(x, self.g)
+        self.ctx.maskit(r)
+        return float(np.sqrt(np.dot(r * self.c, r)) / np.sqrt(np.dot(self.f * self.c, self.f)))
 
 
 def replica_rate(ms, n, niter, steps, world, device=None):
@@ -164,33 +218,46 @@ def replica_rate(ms, n, niter, steps, world, device=None):
     return ms, world * n * niter * steps / (ms / 1e3) / 1e9
 
 
+def workload_config(nel: int, lx: int, niter: int) -> dict:
+    """The workload, identical in both arms' lines."""
+    n = nel ** 3 * lx ** 3
+    return {"workload": f"cg, {nel}^3 elements, lx1={lx}, {niter} FP64 iterations per step",
+            "n": n, "mask": "full Dirichlet", "rhs": "seeded uniform[-1,1] per global DOF",
+            "l2": f"inputs larger than L2 ({8 * n / 1e6:.0f} MB per vector)"}
+
+
 def run_reference(a, rank, world):
+    """The reference's CPU algorithm (the oracle port, OpenMP over elements,
+    every host thread) on the headline mesh and right-hand side; each step
+    is a bounded sample of --cpu-sample-iters CG iterations of that solve."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    nel, iters = a.cpu_sample_nel, a.cpu_sample_iters
-    for _ in range(a.warmup):
-        cpu_rate(nel, a.lx, 1, threads)
-    rates, times = [], []
     t_all = time.perf_counter()
+    case = CpuCase(a.nel, a.lx, threads)
+    for _ in range(a.warmup):
+        case.rate(1)
+    rates, times = [], []
+    t_steps = time.perf_counter()
     for _ in range(a.steps):
-        r, dt, n = cpu_rate(nel, a.lx, iters, threads)
+        r, dt = case.rate(a.cpu_sample_iters)
         rates.append(r)
         times.append(dt)
-    wall = time.perf_counter() - t_all
+    steps_s = time.perf_counter() - t_steps
     v = float(np.median(rates))
-    sample = f"{nel}^3 elements, lx1={a.lx} (n={n}), {iters} CG iterations per step"
+    sample = (f"{a.nel}^3 elements, lx1={a.lx} (n={case.n}), the headline solve's first "
+              f"{a.cpu_sample_iters} CG iterations per step")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": float(np.median(times)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"cg, {a.nel}^3 elements, lx1={a.lx}, {a.niter} iterations",
-                       "sample": sample, "l2": "inputs larger than L2"},
+            "config": workload_config(a.nel, a.lx, a.niter),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "setup_s": case.setup_s, "steps_s": steps_s,
+            "wall_s": time.perf_counter() - t_all}
     print(json.dumps(line), flush=True)
 
 
@@ -209,11 +276,14 @@ def _time_on(stream, torch, fn, reps=10):
     return e0.elapsed_time(e1) / reps
 
 
-def extras(nb, torch, dev):
+def extras(nb, torch, dev, order=2):
     """Deformed-geometry operator error per lx1 (16^3 elements) for the
-    CUDA-core FP32 and the tensor-core (FP16 hi+lo split) operators, with
-    each operator's time, and hsmg-preconditioned CG against plain CG (16^3
-    deformed, lx1=12, levels 12 -> 6 -> 3), to relative residual 1e-10."""
+    CUDA-core FP32 and the tensor-core (FP16 hi+lo split) operators and the
+    FP64 operator in fixed point, each against the FP64 operator in the
+    reference's summation order, with each operator's time; and
+    hsmg-preconditioned CG against plain CG (16^3 deformed, lx1=12, levels
+    12 -> 6 -> 3), to relative residual 1e-10, with the FP64 operator form
+    `order`."""
     res = {"deformed_operator_error": {}, "hsmg_pcg": {}}
     stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
     for lx in (8, 12, 16):
@@ -226,6 +296,10 @@ def extras(nb, torch, dev):
         w64 = torch.empty_like(u)
         m.set_order(0)
         m.ax(w64.data_ptr(), u.data_ptr(), g.data_ptr())
+        wfx = torch.empty_like(u)
+        m.set_order(2)
+        m.ax(wfx.data_ptr(), u.data_ptr(), g.data_ptr())
+        t_fx = _time_on(stream, torch, lambda: m.ax(wfx.data_ptr(), u.data_ptr(), g.data_ptr()))
         m.set_order(1)
         w32 = torch.empty(n, dtype=torch.float32, device=dev)
         u32, g32 = u.float(), g.float()
@@ -236,19 +310,23 @@ def extras(nb, torch, dev):
         sc = w64.abs().max().item()
         d = (w32.double() - w64).abs().max().item() / sc
         dtc = (wtc.double() - w64).abs().max().item() / sc
+        dfx = (wfx - w64).abs().max().item() / sc
         ms = {
             "fp64": _time_on(stream, torch, lambda: m.ax(w64.data_ptr(), u.data_ptr(), g.data_ptr())),
+            "fp64_fixed_point": t_fx,
             "fp32": _time_on(stream, torch,
                              lambda: m.ax_f32(w32.data_ptr(), u32.data_ptr(), g32.data_ptr())),
             "tc": _time_on(stream, torch,
                            lambda: m.ax_tc(wtc.data_ptr(), u32.data_ptr(), g32.data_ptr())),
         }
-        res["deformed_operator_error"][f"lx1={lx}"] = {"fp32": d, "tc": dtc, "n": n,
+        res["deformed_operator_error"][f"lx1={lx}"] = {"fp32": d, "tc": dtc,
+                                                       "fp64_fixed_point": dfx, "n": n,
                                                        "apply_ms": ms}
-        del g, u, w64, w32, u32, g32, wtc
+        del g, u, w64, wfx, w32, u32, g32, wtc
         m.close()
         torch.cuda.empty_cache()
     m = nb.DeviceMesh(16, 16, 16, 12, mask_mode=1)
+    m.set_order(order)
     n = m.n
     g = torch.empty(6 * n, dtype=torch.float64, device=dev)
     c = torch.empty(n, dtype=torch.float64, device=dev)
@@ -299,7 +377,8 @@ def extras(nb, torch, dev):
         tp = time.perf_counter() - t0
         res["hsmg_pcg"][f"pcg_fp{prec}_smoother_exact_coarse_12_6_2"] = {
             "iters": it, "relres": rr, "s": tp, "setup_s": tset}
-    res["hsmg_pcg"]["workload"] = "16^3 deformed elements, lx1=12, levels 12->6->3, tol 1e-10"
+    res["hsmg_pcg"]["workload"] = ("16^3 deformed elements, lx1=12, levels 12->6->3, tol 1e-10, "
+                                   f"FP64 operator order {order}")
     m.close()
     del g, c, f, x
     torch.cuda.empty_cache()
@@ -389,6 +468,10 @@ class _DevArray:
 
 
 # --------------------------------------------------------------- GPU arm --
+def _host(t):
+    return t.detach().cpu().numpy()
+
+
 def run_ours(a, rank, world, local):
     import torch
     torch.cuda.set_device(local)
@@ -398,10 +481,11 @@ def run_ours(a, rank, world, local):
         dist.init_process_group("nccl", device_id=dev)
     import nekbone_gb300 as nb
 
-    nel, lx, niter = a.nel, a.lx, a.niter
+    nel, lx, niter, order = a.nel, a.lx, a.niter, a.order
     t0 = time.perf_counter()
     mesh = nb.DeviceMesh(nel, nel, nel, lx, mask_mode=1)   # topology built on the device
     setup_s = time.perf_counter() - t0
+    mesh.set_order(order)
     setup_host_s = None
     if not a.no_extras and world == 1:
         # the same mesh with jl's sort-based topology on the host, for comparison
@@ -417,7 +501,7 @@ def run_ours(a, rank, world, local):
     f = torch.empty(n, dtype=torch.float64, device=dev)
     mesh.setup_g(g.data_ptr())
     mesh.set_multiplicity(c.data_ptr())
-    mesh.rhs_uniform(f.data_ptr(), c.data_ptr(), 20260 + rank)
+    mesh.rhs_uniform(f.data_ptr(), c.data_ptr(), RHS_SEED + rank)
     x, r, w, p, z = (torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(5))
     ptrs = [t.data_ptr() for t in (x, f, g, c, r, w, p, z)]
     stream = torch.cuda.ExternalStream(nb.stream_handle(), device=dev)
@@ -446,33 +530,49 @@ def run_ours(a, rank, world, local):
     unique = ((lx - 1) * nel + 1) ** 3
     clocks = clk.summary()
     ms_per_step = ms / a.steps
-    launches_per_step = 2 + 3 * niter  # copy/mask/glsc3 + 3 kernels per iteration
+    # per step: x = 0 / r = mask(f) / r'Cr (3), the fixed-point metric (order 2),
+    # then 3 kernels per iteration
+    launches_per_step = 3 + (1 if order == 2 else 0) + 3 * niter
+    x100 = _host(x) if rank == 0 and world == 1 and not a.no_cpu else None
 
-    # dominant kernel timing (the fused element operator) on the same stream
-    kms = mesh.time_cg_kernels(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
-                               r.data_ptr(), w.data_ptr(), p.data_ptr(), reps=10)
+    # each kernel of one iteration on the same stream, for both FP64
+    # operator forms on the integer / FP64 pipes (the chosen one first)
+    kms = {}
+    for o in [order] + [q for q in (2, 1) if q != order]:
+        mesh.set_order(o)
+        kms[o] = mesh.time_cg_kernels(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
+                                      r.data_ptr(), w.data_ptr(), p.data_ptr(), reps=10)
+    mesh.set_order(order)
     ax_bytes = 64 * n   # u 8 + g 48 + w 8 per point (ax, stored metric)
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    achieved = ax_bytes / (kms[0] * 1e-3) / 1e9
+    rates = nb.pipe_rates()
+    achieved = ax_bytes / (kms[order][0] * 1e-3) / 1e9
     flops_pt = 19 + 12 * lx
-    eo = lx % 2 == 0
+    names = {2: f"k_ax_fx<{lx},1> (fused FP64 element operator in 64-bit fixed point on the "
+                f"integer pipes, even-odd contractions)",
+             1: f"k_ax_eo4<double,{lx},1> (fused FP64 element operator, even-odd contractions "
+                f"on the FP64 pipe)",
+             0: f"k_ax_impl<double,{lx},1,false> (fused FP64 element operator, reference order)"}
+    trf = DRAM_BYTES_PER_POINT.get(order) if lx == 12 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak,
-                # DRAM bytes per launch: ncu capture of the same kernel on 16^3
-                # elements (92.2 B per point read + written), scaled by n
-                "traffic": DRAM_BYTES_PER_POINT_AX_EO * n if (eo and lx == 12) else None,
-                "kernel": (f"k_ax_eo4<double,{lx},1> (fused element operator, even-odd "
-                           f"contractions, four CTAs per SM)") if (eo and lx == 12) else
-                          f"k_ax_eo<double,{lx},1> (fused element operator, even-odd contractions)"
-                          if eo else f"k_ax_impl<double,{lx},1,false> (fused element operator)",
+                "traffic": trf[0] * n if trf else None,
+                "traffic_source": trf[1] if trf else None,
+                "kernel": names[order],
+                "algorithmic_bytes_per_point": 64,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback",
-                "kernel_ms": {"ax": kms[0], "gs_fin": kms[1], "update": kms[2]},
-                # the binding resource: the FP64 pipe (GB300 FP64 = 1/72 of FP32)
-                "fp64_pipe": {"reference_flops_per_point": flops_pt,
-                              "tflops_reference_count": flops_pt * n / (kms[0] * 1e-3) / 1e12,
-                              "peak_tflops": FP64_PEAK_TFLOPS,
-                              "ncu_pipe_active": 0.919 if (eo and lx == 12) else None}}
+                "kernel_ms": {"ax": kms[order][0], "gs_fin": kms[order][1],
+                              "update": kms[order][2]},
+                "iteration_ms_by_operator": {
+                    ("fixed_point" if o == 2 else "fp64_pipe" if o == 1 else "reference_order"):
+                        {"ax": kms[o][0], "gs_fin": kms[o][1], "update": kms[o][2],
+                         "iteration": float(sum(kms[o]))} for o in kms},
+                # live issue rates of the pipes (nb_pipe_rates) and the reference's flop
+                # count per point (cg.f:122) at the operator's time
+                "pipes": {"measured_ops_per_s": rates,
+                          "reference_flops_per_point": flops_pt,
+                          "tflops_reference_count": flops_pt * n / (kms[order][0] * 1e-3) / 1e12}}
 
     # the FP32 iteration of the mixed solver's inner CG, same mesh
     f32, g32, c32 = f.float(), g.float(), c.float()
@@ -492,63 +592,110 @@ def run_ours(a, rank, world, local):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
            "warmup": a.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"cg, {nel}^3 elements, lx1={lx}, {niter} FP64 iterations per step",
-                      "n": n, "mask": "full Dirichlet", "rhs": "seeded uniform[-1,1] per global DOF",
-                      "l2": "inputs larger than L2 (453 MB per vector)", "setup_s": setup_s,
-                      "setup_host_topology_s": setup_host_s,
-                      # unique global DOFs of the box, (N nelx + 1)(N nely + 1)(N nelz + 1)
-                      "unique_dofs": unique, "value_unique_gdof_iter_per_s": value * unique / n},
+           "config": workload_config(nel, lx, niter),
+           "operator_order": order,
+           "setup": {"device_topology_s": setup_s, "host_topology_s": setup_host_s,
+                     # unique global DOFs of the box, (N nelx + 1)(N nely + 1)(N nelz + 1)
+                     "unique_dofs": unique, "value_unique_gdof_iter_per_s": value * unique / n},
            "gpu_launches": launches_per_step * a.steps, "clocks": clocks, "roofline": roofline}
+
+    # ---- the CPU oracle on the same mesh and inputs (rank 0, one GPU)
+    case = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        case = CpuCase(nel, lx, threads)
+        assert np.array_equal(case.g, _host(g)) and np.array_equal(case.c, _host(c))
+        assert np.array_equal(case.f, _host(f))
+        ok, dt = case.cg(a.cpu_sample_iters)
+        v = n * a.cpu_sample_iters / dt / 1e9
+        # the GPU's iterate after the same number of iterations
+        mesh.cg(*ptrs, a.cpu_sample_iters)
+        nb.sync()
+        xk = _host(x)
+        scale_f = float(np.max(np.abs(case.f)))
+        out["cpu_check"] = {
+            "iterate_iters": a.cpu_sample_iters,
+            "x_rel_err": float(np.max(np.abs(xk - ok["x"])) / np.max(np.abs(ok["x"]))),
+            "r_err_on_f_scale": float(np.max(np.abs(_host(r) - ok["r"])) / scale_f),
+            "headline_x_cpu_relres": case.relres(x100),
+            "oracle_setup_s": case.setup_s}
+        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                               "sample": f"{nel}^3 elements, lx1={lx} (n={n}), the headline "
+                                         f"solve's first {a.cpu_sample_iters} FP64 CG iterations, "
+                                         f"{dt:.1f} s"}
+        # the same port on one core (the reference has no threading of its own)
+        case.ctx.set_threads(1)
+        v1, dt1 = case.rate(1)
+        case.ctx.set_threads(threads)
+        out["cpu_baseline_single_core"] = {
+            "value": v1, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{nel}^3 elements, lx1={lx} (n={n}), 1 FP64 CG iteration, {dt1:.1f} s"}
 
     # ---- mixed vs FP64 time to tolerance
     if not a.no_mixed:
         xt = torch.zeros(n, dtype=torch.float64, device=dev)
+        xm = torch.zeros(n, dtype=torch.float64, device=dev)
+        args = (f.data_ptr(), g.data_ptr(), c.data_ptr())
         # one untimed solve of each kind first (first-use scratch allocation,
         # kernel loading), as the FP64 headline has its warm-up steps
-        mesh.cg_tol(xt.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol,
-                    max_iter=20000, check_every=50)
-        mesh.cg_mixed(xt.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol, 20, 5000)
-        xt.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        it64, rr64 = mesh.cg_tol(xt.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol,
-                                 max_iter=20000, check_every=50)
-        t64 = time.perf_counter() - t0
-        xm = torch.zeros(n, dtype=torch.float64, device=dev)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        outer, inner, rrm = mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
-                                          a.tol, 20, 5000)
-        tm = time.perf_counter() - t0
-        diff = float((xm - xt).abs().max().item() / max(xt.abs().max().item(), 1e-300))
-        out["mixed"] = {"tol": a.tol, "fp64_s": t64, "fp64_iters": it64, "fp64_relres": rr64,
-                        "mixed_s": tm, "mixed_outer": outer, "mixed_inner_iters": inner,
-                        "mixed_relres": rrm, "speedup": t64 / tm, "x_rel_diff": diff}
-        # the same solve with the inner element products on the tensor cores
-        # (FP16 hi+lo split operands, FP32 accumulation; unfused iteration)
-        nb.set_mixed_tensor_cores(True)
-        try:
-            xm.zero_()
-            mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), a.tol, 20, 5000)
-            xm.zero_()
+        mesh.cg_tol(xt.data_ptr(), *args, a.tol, max_iter=20000, check_every=1)
+        mesh.cg_mixed(xm.data_ptr(), *args, a.tol, 20, 5000)
+
+        def timed(fn):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            o_tc, i_tc, rr_tc = mesh.cg_mixed(xm.data_ptr(), f.data_ptr(), g.data_ptr(),
-                                              c.data_ptr(), a.tol, 20, 5000)
-            t_tc = time.perf_counter() - t0
+            res = fn()
+            torch.cuda.synchronize()
+            return res, time.perf_counter() - t0
+
+        # FP64 CG polled every iteration: charged the iterations it needs
+        xt.zero_()
+        (it64, rr64), t64 = timed(lambda: mesh.cg_tol(xt.data_ptr(), *args, a.tol,
+                                                      max_iter=20000, check_every=1))
+        mx = {}
+        try:
+            for key, shared, tc in (("per_element_metric", False, False),
+                                    ("shared_metric_block", True, False),
+                                    ("tensor_cores", False, True)):
+                nb.set_shared_metric(shared)
+                nb.set_mixed_tensor_cores(tc)
+                if tc:
+                    mesh.cg_mixed(xm.data_ptr(), *args, a.tol, 20, 5000)   # warm-up
+                xm.zero_()
+                (o_, i_, rr_), t_ = timed(lambda: mesh.cg_mixed(xm.data_ptr(), *args, a.tol,
+                                                                20, 5000))
+                d = float((xm - xt).abs().max().item() / max(xt.abs().max().item(), 1e-300))
+                mx[key] = {"s": t_, "outer": o_, "inner_iters": i_, "relres": rr_,
+                           "speedup_vs_fp64": t64 / t_, "x_rel_diff_vs_fp64": d}
+                if case is not None:
+                    mx[key]["cpu_relres"] = case.relres(_host(xm))
         finally:
+            nb.set_shared_metric(True)
             nb.set_mixed_tensor_cores(False)
-        d_tc = float((xm - xt).abs().max().item() / max(xt.abs().max().item(), 1e-300))
-        out["mixed"]["tensor_cores"] = {"s": t_tc, "outer": o_tc, "inner_iters": i_tc,
-                                        "relres": rr_tc, "speedup_vs_fp64": t64 / t_tc,
-                                        "x_rel_diff": d_tc}
+        fp64 = {"s": t64, "iters": it64, "relres": rr64, "check_every": 1}
+        if case is not None:
+            fp64["cpu_relres"] = case.relres(_host(xt))
+        out["mixed_detail"] = {"tol": a.tol, "fp64_cg": fp64, **mx,
+                               "note": "per_element_metric is the headline mixed figure: "
+                                       "the inner FP32 operator reads each element's metric; "
+                                       "shared_metric_block reads one block for all (box "
+                                       "meshes only) and is reported separately"}
+        out["_mixed"] = {"tol": a.tol, "fp64_s": t64, "fp64_iters": it64,
+                         "mixed_s": mx["per_element_metric"]["s"],
+                         "speedup": mx["per_element_metric"]["speedup_vs_fp64"],
+                         "mixed_relres": mx["per_element_metric"]["relres"],
+                         "cpu_relres_fp64": fp64.get("cpu_relres"),
+                         "cpu_relres_mixed": mx["per_element_metric"].get("cpu_relres"),
+                         "speedup_shared_metric": mx["shared_metric_block"]["speedup_vs_fp64"],
+                         "speedup_tensor_cores": mx["tensor_cores"]["speedup_vs_fp64"]}
         del xt, xm
+    case = None
 
     # ---- the other workloads, one measurement each (not the headline)
     if not a.no_extras and world == 1:
         del x, r, w, p, z
         torch.cuda.empty_cache()
-        out["extras"] = extras(nb, torch, dev)
+        out["extras"] = extras(nb, torch, dev, order)
         x = r = w = p = z = None
 
     # ---- end to end through the drop-in cg_ with pinned host buffers
@@ -556,6 +703,7 @@ def run_ours(a, rank, world, local):
         x = r = w = p = z = None
         torch.cuda.empty_cache()
         hb = nb.Nekbone(nel, nel, nel, lx, mask_mode=1)
+        nb.Nekbone.set_order(order)
         pin = lambda t: t.cpu().pin_memory()
         fh, gh, ch = pin(f), pin(g), pin(c)
         work = [torch.zeros(n, dtype=torch.float64).pin_memory() for _ in range(5)]
@@ -577,19 +725,8 @@ def run_ours(a, rank, world, local):
                       "calls_ms": [round(v, 2) for v in calls],
                       "clocks": clk_e2e.summary()}
 
-    if rank == 0 and world == 1 and not a.no_cpu:
-        threads = os.cpu_count() or 1
-        v, dt, ns = cpu_rate(a.cpu_sample_nel, lx, a.cpu_sample_iters, threads)
-        out["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                               "sample": f"{a.cpu_sample_nel}^3 elements, lx1={lx} (n={ns}), "
-                                         f"{a.cpu_sample_iters} FP64 CG iterations, {dt:.1f} s"}
-        # the same port on one core (the reference has no threading of its own)
-        it1 = max(2, a.cpu_sample_iters // threads)
-        v1, dt1, _ = cpu_rate(a.cpu_sample_nel, lx, it1, 1)
-        out["cpu_baseline_single_core"] = {
-            "value": v1, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{a.cpu_sample_nel}^3 elements, lx1={lx} (n={ns}), {it1} FP64 CG "
-                      f"iterations, {dt1:.1f} s"}
+    if "_mixed" in out:
+        out["mixed"] = out.pop("_mixed")       # last key: the driver's tail shows it
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:

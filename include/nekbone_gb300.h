@@ -263,7 +263,10 @@ int nb_cg_tol(nb_mesh *mesh, double *x, const double *f, const double *g,
  * device array of the library (about 128 KiB per GPU that loads it, held
  * until exit), so n must not exceed NB_NOALLOC_MAX_N.  Calls share that
  * array: calls that overlap on the GPU race.  The first call on a device
- * looks the array up; make it before any stream capture. */
+ * looks the array up and launches the kernel for the first time, and with
+ * lazy module loading (CUDA's default) that first launch may itself
+ * allocate and synchronise: make one warm-up call per device before the
+ * region that must not allocate, and before any stream capture. */
 #define NB_NOALLOC_MAX_N 67108864L
 int nb_glsc3_noalloc(const double *a, const double *b, const double *mult,
                      long n, double *result, void *stream);
@@ -317,6 +320,13 @@ int nb_wait_selftest(unsigned polls);
  * nb_ax_f32, nb_ax_tc, nb_cg, nb_batch_solve) leave them to the next of
  * those.  No counterpart in the reference. */
 int nb_set_wait_test(int on);
+
+/* Issue rates of the pipes the element operators use, measured on the
+ * current device: rates[0] FP64 fused multiply-adds, rates[1] 32x32->64-bit
+ * integer multiply-adds (mad.wide.s32), rates[2] 32-bit integer adds,
+ * rates[3] FP32 fused multiply-adds, each in operations per second (about
+ * 50 ms).  No counterpart in the reference. */
+int nb_pipe_rates(double *rates);
 
 /* Synchronise the library's stream. */
 int nb_sync(void);

@@ -56,7 +56,7 @@ EXPORTS = (
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
-    "nb_wait_selftest", "nb_set_wait_test",
+    "nb_wait_selftest", "nb_set_wait_test", "nb_pipe_rates",
 )
 
 lib.nekbone_last_status.restype = _i
@@ -132,6 +132,8 @@ lib.nb_wait_selftest.restype = _i
 lib.nb_wait_selftest.argtypes = [_C.c_uint]
 lib.nb_set_wait_test.restype = _i
 lib.nb_set_wait_test.argtypes = [_i]
+lib.nb_pipe_rates.restype = _i
+lib.nb_pipe_rates.argtypes = [_p]
 for _name in ("nb_mesh_gs_maps", "nb_mesh_boundary_groups"):
     getattr(lib, _name).restype = _i
     getattr(lib, _name).argtypes = [_p, _p, _p, _p, _p]
@@ -676,6 +678,15 @@ def set_wait_test(on: bool) -> None:
     """Makes the bulk-copy waits of later launches run out on purpose (the
     timeout path of the real kernels); off restores normal runs."""
     _check(lib.nb_set_wait_test(1 if on else 0))
+
+
+def pipe_rates() -> dict:
+    """Measured operations per second of the FP64 FMA, integer
+    multiply-add (mad.wide.s32), integer add and FP32 FMA pipes."""
+    r = _np.zeros(4)
+    _check(lib.nb_pipe_rates(_ptr(r)))
+    return {"dfma": float(r[0]), "imad_wide": float(r[1]), "iadd": float(r[2]),
+            "ffma": float(r[3])}
 
 
 def stream_handle() -> int:

@@ -295,8 +295,8 @@ void nekbone_set_mgrid_(const int *ifmgrid) { st().mgrid = *ifmgrid != 0; }
 
 void nekbone_set_contraction_order_(const int *order) {
   clear_status();
-  if (*order != 0 && *order != 1) {
-    fail(NB_ERR_ARG, "contraction order %d not 0 or 1", *order);
+  if (*order < 0 || *order > 2) {
+    fail(NB_ERR_ARG, "contraction order %d not 0, 1 or 2", *order);
     return;
   }
   st().order = *order;
@@ -531,6 +531,7 @@ void ax_(double *w, const double *u, const double *gxyz, double *ur,
   double *dw, *du, *dg;
   if (dbuf(0, nn, &dw) || dbuf(1, nn, &du) || dbuf(2, 6 * nn, &dg)) return;
   if (h2d(du, u, nn * 8) || h2d(dg, gxyz, 6 * nn * 8)) return;
+  metric_fx_invalidate(*op);
   if (apply_ax<double>(*op, dw, du, dg, S.s)) return;
   if (d2h(w, dw, nn * 8)) return;
   if (sync()) return;
@@ -881,7 +882,7 @@ int nb_mesh_mask_list(const nb_mesh *mesh, int *n, int *list) {
 int nb_mesh_set_order(nb_mesh *mesh, int order) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
-  if (order != 0 && order != 1) return fail(NB_ERR_ARG, "order %d not 0 or 1", order);
+  if (order < 0 || order > 2) return fail(NB_ERR_ARG, "order %d not 0, 1 or 2", order);
   mesh->op.order = order;
   return NB_OK;
 }
@@ -955,6 +956,7 @@ int nb_rhs_uniform(nb_mesh *mesh, double *f, const double *c, uint64_t seed) {
 int nb_ax(nb_mesh *mesh, double *w, const double *u, const double *g) {
   clear_status();
   if (!mesh) return fail(NB_ERR_HANDLE, "null mesh");
+  metric_fx_invalidate(mesh->op);
   NB_TRY(apply_ax<double>(mesh->op, w, u, g, st().s));
   return NB_OK;
 }

@@ -1,0 +1,431 @@
+// nb_ax_fx.cuh -- the FP64 element operator (ax_e, cg.f:142-168, with
+// local_grad3 / local_grad3_t, cg.f:170-212) evaluated in 64-bit fixed
+// point on the integer pipes instead of GB300's FP64 pipe.
+//
+// GB300 executes about 0.5e12 FP64 fused multiply-adds per second, but
+// about 14e12 32x32->64-bit integer multiply-adds (mad.wide.s32) and 19e12
+// simple integer operations (measured).  A product of two 60-bit
+// fixed-point numbers built from three mad.wide.s32 therefore costs a tenth
+// of one DFMA.  So this operator keeps its values as block-floating-point
+// integers and leaves only the CG vector arithmetic (p update, +0.1 p, pap)
+// on the FP64 pipe:
+//
+//  * each element's input p is scaled by one power of two chosen from the
+//    element's largest exponent and rounded to an integer P, |P| < 2^59
+//    (to_fixed); the derivative tables are fixed-point integers with FC
+//    fractional bits (|C| <= 2^58, rounded once on the host from D's exact
+//    value); the metric g is converted once per solve, one exponent per
+//    element (|G| < 2^60);
+//  * a product a*b of two such integers is formed from balanced 32-bit
+//    halves, a = ah 2^32 + al with al in [-2^31, 2^31):
+//        a*b ~= ah*bh 2^64 + (ah*bl + al*bh) 2^32,
+//    al*bl (|al*bl| <= 2^62, unbiased: al is symmetric) dropped; the terms
+//    of one output are accumulated in two int64 registers (Acc) and
+//    combined once, rounded to units of 2^60 (2^62 for the transposed
+//    gradient, whose three outputs are summed in int64: each is below
+//    2^59.6; 2^64 for the metric step), so one output's error is a few
+//    units, ~2^-57 of its largest product.  The rounding costs nothing (the
+//    accumulator starts at half a unit) and neither does the scaling (the hi
+//    halves of the coefficients come pre-scaled);
+//  * the even-odd split of the GLL derivative (as k_ax_eo) halves the
+//    products: per point and direction 6 multiply-adds at lx1 = 12;
+//  * after the gradient and after the metric step the element's values are
+//    renormalised by one shift (the element-wide OR of the magnitudes gives
+//    the top bit), so every stage works with ~58 significant bits of the
+//    element's largest value;
+//  * the result is converted back to FP64 with round-to-nearest-even by
+//    bit assembly (no FP64 conversion instruction, which runs at the FP64
+//    pipe's rate).
+// This is block floating point: the error of a value is bounded relative to
+// the largest value of its element (~2^-56), where FP64 bounds it relative
+// to the value itself.  Results agree with the reference's FP64 evaluation
+// to rounding (~1e-15 of the element's scale), not bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nb_kernels.cuh"
+
+namespace nb {
+namespace fx {
+
+typedef long long i64;
+typedef unsigned long long u64;
+
+// ------------------------------------------------------------ integers --
+// balanced halves: x = hi * 2^32 + lo, lo in [-2^31, 2^31)
+struct Sp {
+  int lo, hi;
+};
+__device__ __forceinline__ Sp split(i64 x) {
+  Sp s;
+  const unsigned low = unsigned(u64(x));
+  s.lo = int(low);
+  s.hi = int(u64(x) >> 32) + int(low >> 31);
+  return s;
+}
+
+// A sum of products a*b in units of 2^U: hh counts ah*bh 2^(64-U) -- the
+// caller passes ah already scaled by 2^(64-U) (chs) -- and x counts
+// (ah*bl + al*bh) in units of 2^32, started at half a unit of 2^U so that the
+// final shift rounds to nearest (al*bl dropped).
+template <int U>
+struct Acc {
+  i64 hh, x;
+  __device__ __forceinline__ Acc() : hh(0), x(1ll << (U - 33)) {}
+  __device__ __forceinline__ void mac(int chs, int chi, int clo, const Sp &v) {
+    hh += i64(chs) * i64(v.hi);
+    x += i64(chi) * i64(v.lo);
+    x += i64(clo) * i64(v.hi);
+  }
+  __device__ __forceinline__ i64 result() const { return hh + (x >> (U - 32)); }
+};
+
+// v * 2^sh, rounded to nearest for sh < 0
+__device__ __forceinline__ i64 shift_signed(i64 v, int sh) {
+  return sh >= 0 ? i64(u64(v) << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
+}
+
+// ----------------------------------------------------- FP64 <-> fixed --
+__device__ __forceinline__ int bexp(double x) {
+  return int((u64(__double_as_longlong(x)) >> 52) & 0x7FFu);
+}
+
+// x * 2^(1075 - emax + up) rounded to nearest (ties away from zero), for x
+// whose biased exponent is <= emax: |result| < 2^(53 + up)
+__device__ __forceinline__ i64 to_fixed(double x, int emax, int up) {
+  const u64 b = u64(__double_as_longlong(x));
+  const int e = int((b >> 52) & 0x7FFu);
+  const u64 m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
+  const int sh = (e ? e : 1) - emax + up;
+  u64 mag;
+  if (sh >= 0) mag = m << sh;
+  else if (sh > -54) mag = ((m >> (-sh - 1)) + 1ull) >> 1;
+  else mag = 0ull;
+  return (b >> 63) ? -i64(mag) : i64(mag);
+}
+
+// W * 2^s rounded to the nearest FP64 value (ties to even)
+__device__ __forceinline__ double to_double(i64 W, int s) {
+  if (W == 0) return 0.0;
+  const u64 sign = u64(W) & (1ull << 63);
+  u64 mag = W < 0 ? u64(-W) : u64(W);
+  const int lz = __clzll(i64(mag));
+  mag <<= lz;                       // top bit at 63
+  int ex = 63 - lz + s;             // unbiased exponent of the value
+  u64 mant = mag >> 11;             // 53 bits
+  const u64 rem = mag & 0x7FFull;
+  if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ++mant;
+  if (mant >> 53) {
+    mant >>= 1;
+    ++ex;
+  }
+  int be = ex + 1023;
+  if (be >= 2047) return __longlong_as_double(i64(sign | (0x7FFull << 52)));
+  if (be <= 0) {  // subnormal: mant * 2^(ex - 52) with 2^-1074 as the unit
+    const int rs = 1 - be;
+    if (rs > 53) return __longlong_as_double(i64(sign));
+    const u64 half = 1ull << (rs - 1), low = mant & ((1ull << rs) - 1ull);
+    u64 q = mant >> rs;
+    if (low > half || (low == half && (q & 1ull))) ++q;
+    return __longlong_as_double(i64(sign | q));
+  }
+  return __longlong_as_double(i64(sign | (u64(be) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
+
+// ----------------------------------------------------- block reductions --
+// lanes of warp w of an nt-thread block
+__device__ __forceinline__ unsigned warp_mask(int nt, int w) {
+  const int n = nt - 32 * w;
+  return n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u);
+}
+
+// ------------------------------------------------------------ operator --
+// Units of the contraction outputs: the gradient's 2^60, the transposed
+// gradient's 2^62 (its three outputs are summed in int64).
+constexpr int kUGrad = 60, kUGradT = 62;
+
+// Derivative tables in fixed point: E, O of D, then E, O of D^T (the
+// even-odd tables of k_ax_eo, 4*(lx1/2)^2 values, row a), as balanced
+// halves, |coefficient| <= 2^58; hs = hi scaled by 2^(64 - U) of the stage
+// that uses the table.  A kernel parameter, read as multiply-add operands.
+template <int LX>
+struct FxCoef {
+  int hi[4 * (LX / 2) * (LX / 2)];
+  int lo[4 * (LX / 2) * (LX / 2)];
+  int hs[4 * (LX / 2) * (LX / 2)];
+  int fc;  // fractional bits: coefficient = (hi 2^32 + lo) 2^-fc
+};
+
+template <int LX>
+struct FxShared {
+  static constexpr int N = (LX + 1) * LX * LX;
+  i64 A[N];
+  i64 B[N];
+  i64 C[N];
+  int emax[8];
+  unsigned orl[8], orh[8];
+  double red[32];
+};
+
+template <int LX>
+__device__ __forceinline__ int fx_at(int i, int j, int k) {
+  return i + (LX + 1) * j + (LX + 1) * LX * k;
+}
+
+// y(0..n-1) = C v of one line v (fixed point, |v| < 2^59), coefficient
+// tables at offset q0 of cf (E at q0, O at q0 + h^2); y in units of 2^U of
+// the products (|y| < 2^(120.6 - U))
+template <int LX, int U>
+__device__ __forceinline__ void fx_line(const i64 *v, const FxCoef<LX> &cf, int q0, i64 *y) {
+  constexpr int H = LX / 2;
+  Sp ve[H], vo[H];
+#pragma unroll
+  for (int m = 0; m < H; ++m) {
+    ve[m] = split(v[m] + v[LX - 1 - m]);
+    vo[m] = split(v[m] - v[LX - 1 - m]);
+  }
+#pragma unroll
+  for (int a = 0; a < H; ++a) {
+    Acc<U> e, o;
+#pragma unroll
+    for (int m = 0; m < H; ++m) {
+      const int qe = q0 + a * H + m, qo = qe + H * H;
+      e.mac(cf.hs[qe], cf.hi[qe], cf.lo[qe], ve[m]);
+      o.mac(cf.hs[qo], cf.hi[qo], cf.lo[qo], vo[m]);
+    }
+    const i64 ye = e.result(), yo = o.result();
+    y[a] = ye + yo;
+    y[LX - 1 - a] = yo - ye;
+  }
+}
+
+// OR of the magnitudes of a thread's values, combined over the block after
+// the next __syncthreads (fx_or_read): its top bit is the largest's
+__device__ __forceinline__ void fx_or_post(u64 v, unsigned *orl, unsigned *orh, int t, int nt) {
+  const int w = t >> 5;
+  const unsigned msk = warp_mask(nt, w);
+  const unsigned l = __reduce_or_sync(msk, unsigned(v)), h = __reduce_or_sync(msk, unsigned(v >> 32));
+  if ((t & 31) == 0) {
+    orl[w] = l;
+    orh[w] = h;
+  }
+}
+// the shift that brings the block's largest magnitude below 2^59
+__device__ __forceinline__ int fx_or_shift(const unsigned *orl, const unsigned *orh, int nt) {
+  u64 v = 0;
+  for (int w = 0; w < (nt + 31) / 32; ++w) v |= (u64(orh[w]) << 32) | orl[w];
+  if (v == 0) return 0;
+  return 58 - (63 - __clzll(i64(v)));
+}
+// one's complement magnitude: the same top bit as |v| (one lower for an
+// exact negative power of two, which the bounds leave room for)
+__device__ __forceinline__ u64 mag(i64 v) { return u64(v ^ (v >> 63)); }
+
+// MODE 0 / 1 / 2 as k_ax_eo (AxArgs); a.gfx / a.gexp hold the metric in
+// fixed point (metric_fx_prepare).
+template <int LX, int MODE>
+__device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef<LX> &cf) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  FxShared<LX> &sm = *reinterpret_cast<FxShared<LX> *>(smem_raw);
+  constexpr int L2 = LX * LX, L3 = LX * LX * LX, H = LX / 2;
+  const int t = threadIdx.x + LX * threadIdx.y;
+  const int i = threadIdx.x, j = threadIdx.y;  // own column (i,j)
+  const int e = blockIdx.x;
+  const size_t base = size_t(e) * L3;
+  const int fc = cf.fc;
+
+  // direction update (MODE 1) / correction (MODE 2), in FP64, then the
+  // element's exponent and its fixed-point block
+  int em = 0;
+  {
+    double uk[LX];
+    double pold[LX];
+    const double beta = (MODE == 1 && !a.first) ? a.sc->beta : 0.0;
+#pragma unroll
+    for (int k = 0; k < LX; ++k) {  // all loads before the first store
+      const size_t id = base + size_t(k) * L2 + t;
+      if (MODE == 1) {
+        uk[k] = a.u[id];
+        pold[k] = a.first ? 0.0 : a.p[id];
+      } else if (MODE == 2) {
+        uk[k] = a.p[id];
+        pold[k] = a.e ? double(a.e[id]) : 0.0;
+      } else {
+        uk[k] = a.u[id];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < LX; ++k) {
+      const size_t id = base + size_t(k) * L2 + t;
+      if (MODE == 1) {
+        if (!a.first) uk[k] = fma_rn(beta, pold[k], uk[k]);  // add2s1, math.f:534
+        a.p[id] = uk[k];
+      } else if (MODE == 2 && a.e) {
+        uk[k] = fma_rn(a.scale, pold[k], uk[k]);
+        a.p[id] = uk[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < LX; ++k) em = max(em, bexp(uk[k]));
+    const int w = t >> 5;
+    const int r = __reduce_max_sync(warp_mask(L2, w), unsigned(em));
+    if ((t & 31) == 0) sm.emax[w] = r;
+    __syncthreads();
+    em = 0;
+    for (int q = 0; q < (L2 + 31) / 32; ++q) em = max(em, sm.emax[q]);
+#pragma unroll
+    for (int k = 0; k < LX; ++k) sm.A[fx_at<LX>(i, j, k)] = to_fixed(uk[k], em, 6);
+  }
+  const int sP = em - 1081;  // p = P 2^sP
+  __syncthreads();
+
+  // gradient (local_grad3): thread (i,j) takes the r-line (j=i, k=j) and the
+  // s-line (i, k=j) (consecutive threads on distinct banks), from A into B
+  // and C, and its own column, the t-line (i,j), into registers
+  u64 orv = 0;
+  i64 col[LX];
+  {
+    i64 v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(m, i, j)];  // r-line
+    fx_line<LX, kUGrad>(v, cf, 0, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) {
+      sm.B[fx_at<LX>(m, i, j)] = y[m];
+      orv |= mag(y[m]);
+    }
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, m, j)];  // s-line
+    fx_line<LX, kUGrad>(v, cf, 0, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) {
+      sm.C[fx_at<LX>(i, m, j)] = y[m];
+      orv |= mag(y[m]);
+    }
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, j, m)];  // t-line
+    fx_line<LX, kUGrad>(v, cf, 0, col);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) orv |= mag(col[m]);
+  }
+  fx_or_post(orv, sm.orl, sm.orh, t, L2);
+  __syncthreads();
+  const int s1 = fx_or_shift(sm.orl, sm.orh, L2);
+  const int sU = sP - fc + kUGrad - s1;  // ur = UR 2^sU after the shift
+
+  // metric (cg.f:156-163) at the thread's own points: G (balanced halves)
+  // times the gradient, products in units of 2^64
+  const int eg = a.gexp[e];
+  const int sW = 64 + (eg - 1082) + sU;  // wr = WR 2^sW before renormalising
+  orv = 0;
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = fx_at<LX>(i, j, k);
+    const Sp ur = split(shift_signed(sm.B[q], s1)), us = split(shift_signed(sm.C[q], s1)),
+             ut = split(shift_signed(col[k], s1));
+    const int4 *gp = reinterpret_cast<const int4 *>(a.gfx + 6 * (base + size_t(k) * L2 + t));
+    const int4 g01 = __ldg(gp), g23 = __ldg(gp + 1), g45 = __ldg(gp + 2);
+    const Sp G1 = {g01.x, g01.y}, G2 = {g01.z, g01.w}, G3 = {g23.x, g23.y},
+             G4 = {g23.z, g23.w}, G5 = {g45.x, g45.y}, G6 = {g45.z, g45.w};
+    Acc<64> wr, ws, wt;
+    wr.mac(G1.hi, G1.hi, G1.lo, ur); wr.mac(G2.hi, G2.hi, G2.lo, us); wr.mac(G3.hi, G3.hi, G3.lo, ut);
+    ws.mac(G2.hi, G2.hi, G2.lo, ur); ws.mac(G4.hi, G4.hi, G4.lo, us); ws.mac(G5.hi, G5.hi, G5.lo, ut);
+    wt.mac(G3.hi, G3.hi, G3.lo, ur); wt.mac(G5.hi, G5.hi, G5.lo, us); wt.mac(G6.hi, G6.hi, G6.lo, ut);
+    const i64 r_ = wr.result(), s_ = ws.result(), t_ = wt.result();
+    sm.B[q] = r_;
+    sm.C[q] = s_;
+    col[k] = t_;
+    orv |= mag(r_) | mag(s_) | mag(t_);
+  }
+  fx_or_post(orv, sm.orl, sm.orh, t, L2);
+  __syncthreads();
+  const int s2 = fx_or_shift(sm.orl, sm.orh, L2);
+  const int sT = kUGradT - fc + sW - s2;  // transposed-gradient outputs: value 2^sT
+
+  // transposed gradient (local_grad3_t) with D^T: tr into A, ts into B
+  // (after every r-line of B was read), tt in registers
+  {
+    i64 v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.B[fx_at<LX>(m, i, j)], s2);
+    fx_line<LX, kUGradT>(v, cf, 2 * H * H, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.A[fx_at<LX>(m, i, j)] = y[m];  // tr
+  }
+  __syncthreads();
+  {
+    i64 v[LX], y[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.C[fx_at<LX>(i, m, j)], s2);
+    fx_line<LX, kUGradT>(v, cf, 2 * H * H, y);
+#pragma unroll
+    for (int m = 0; m < LX; ++m) sm.B[fx_at<LX>(i, m, j)] = y[m];  // ts
+  }
+  {
+    i64 v[LX];
+#pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = shift_signed(col[m], s2);
+    fx_line<LX, kUGradT>(v, cf, 2 * H * H, col);  // tt
+  }
+  __syncthreads();
+
+  // w_L = tr + ts + tt in FP64; the CG epilogue as k_ax_eo's.  The
+  // interior's p (written above by this thread, so in cache), c and f are
+  // read again here rather than held in registers through the contractions.
+  const bool col_interior = (i > 0) && (i < LX - 1) && (j > 0) && (j < LX - 1);
+  double part = 0.0;
+  double pk[LX], ck[LX], fk[LX];
+  if (MODE != 0 && col_interior) {
+#pragma unroll
+    for (int k = 1; k < LX - 1; ++k) {  // all loads before the first store
+      const size_t id = base + size_t(k) * L2 + t;
+      pk[k] = a.p[id];
+      ck[k] = __ldg(a.c + id);
+      if (MODE == 2) fk[k] = __ldg(a.f + id);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < LX; ++k) {
+    const int q = fx_at<LX>(i, j, k);
+    double wl = to_double(sm.A[q] + sm.B[q] + col[k], sT);
+    const size_t id = base + size_t(k) * L2 + t;
+    const bool interior = col_interior && (k > 0) && (k < LX - 1);
+    if (MODE == 1) {
+      if (interior) {
+        wl = fma_rn(0.1, pk[k], wl);
+        part = fma_rn(mul_rn(wl, ck[k]), pk[k], part);
+      }
+      a.w[id] = wl;
+    } else if (MODE == 2) {
+      if (interior) {
+        const double rv = fk[k] - fma_rn(0.1, pk[k], wl);
+        a.r[id] = rv;
+        part = fma_rn(mul_rn(rv, ck[k]), rv, part);
+      } else {
+        a.w[id] = wl;
+      }
+    } else {
+      a.w[id] = wl;
+    }
+  }
+  if (MODE != 0) {
+    const double s = block_sum<double>(part, sm.red);
+    if (t == 0) a.partial[e] = s;
+  }
+}
+
+template <int LX, int MODE>
+__global__ void __launch_bounds__(LX * LX, (LX <= 12 ? 4 : 1))
+    k_ax_fx(AxArgs<double> a, const __grid_constant__ FxCoef<LX> cf) {
+  ax_fx_body<LX, MODE>(a, cf);
+}
+
+template <int LX>
+constexpr size_t ax_fx_smem_bytes() {
+  return sizeof(FxShared<LX>);
+}
+
+}  // namespace fx
+}  // namespace nb

@@ -1,0 +1,8 @@
+// nb_ax_fx_m2.cu -- fixed-point FP64 element operator, MODE 2.
+#include "nb_ax_fx_launch.cuh"
+
+namespace nb {
+int launch_ax_fx_m2(const Operator &op, AxArgs<double> a, cudaStream_t s) {
+  return launch_ax_fx_mode<2>(op, a, s);
+}
+}  // namespace nb

@@ -121,6 +121,8 @@ struct AxArgs {
   unsigned *err;     // device error word for bounded waits (may be null)
   int g_uniform;     // every element's metric block equals element 0's: read that one
   int wait_test;     // timeout self-test of the bulk-copy wait (block_copy_begin)
+  const int2 *gfx;   // fixed-point FP64 operator: the metric in fixed point
+  const int *gexp;   //   and each element's exponent (metric_fx_prepare)
 };
 
 template <typename T, int LX>

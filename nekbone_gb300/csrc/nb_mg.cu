@@ -1379,6 +1379,7 @@ static int coarse_rap(Multigrid &mg, const double *g, double *x1, double *z, dou
   NB_CUDA(cudaMemsetAsync(z, 0, op.n * sizeof(double), s));
   NB_TRY(mg_intp_add<double>(mg, z, src, L - 1, false, s));
   // A
+  metric_fx_invalidate(op);
   NB_TRY(apply_ax<double>(op, w, z, g, s));
   // R: the downward leg, masked at every level as h1mg_schwarz masks r
   MgLevel &Top = mg.lv[L];

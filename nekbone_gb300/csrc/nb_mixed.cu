@@ -249,6 +249,7 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   // reduction buffers (this may be the mesh's first solve), then scratch:
   // r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32 (FP32); one int flag
   int st = wk.ensure(op, std::max(inner_iters, 1));
+  metric_fx_invalidate(op);
   if (!st) st = wk.ensure_scratch(size_t(n) * (2 * 8 + 12 * 4) + 16);
   if (st) return st;
   double *r = reinterpret_cast<double *>(wk.scratch);

@@ -17,8 +17,15 @@
 //    Calls that overlap on the GPU (different streams, no ordering between
 //    them) race on the array and give wrong sums.
 //  * The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current.  Make that first call
-//    before any stream capture begins.
+//    (cudaGetSymbolAddress) with that device current, and is the first
+//    launch of the kernel.  Under lazy module loading (the default since
+//    CUDA 12.2) that first launch loads the module, which can itself
+//    allocate device memory and synchronise.  So make one warm-up call per
+//    device before the region that must not allocate, and before any stream
+//    capture begins.  The address cache is safe against concurrent first
+//    calls from several host threads.
+#include <atomic>
+
 #include "../../include/nekbone_gb300.h"
 #include "nb_internal.h"
 #include "nb_kernels.cuh"
@@ -36,7 +43,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch
     [kNoAllocMaxParts * sizeof(double) + 256];
 
 constexpr int kMaxDevices = 64;
-void *g_scratch_ptr[kMaxDevices] = {nullptr};
+std::atomic<void *> g_scratch_ptr[kMaxDevices];  // zero-initialised (static storage)
 
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_glsc3_noalloc(const double *__restrict__ a, const double *__restrict__ b,
@@ -64,15 +71,16 @@ int scratch_address(void **out) {
   NB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices)
     return fail(NB_ERR_UNSUPPORTED, "nb_glsc3_noalloc: device %d out of range", dev);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
+  void *p = g_scratch_ptr[dev].load(std::memory_order_acquire);
+  if (!p) {
+    // concurrent first calls may both look it up; they store the same address
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess)
       return fail(NB_ERR_CUDA, "nb_glsc3_noalloc: cudaGetSymbolAddress: %s",
                   cudaGetErrorString(e));
-    g_scratch_ptr[dev] = p;
+    g_scratch_ptr[dev].store(p, std::memory_order_release);
   }
-  *out = g_scratch_ptr[dev];
+  *out = p;
   return NB_OK;
 }
 

@@ -27,6 +27,8 @@ Operator::~Operator() {
   if (d_face) cudaFree(d_face);
   if (bnd_off) cudaFree(bnd_off);
   if (bnd_idx) cudaFree(bnd_idx);
+  if (gfx) cudaFree(gfx);
+  if (gexp) cudaFree(gexp);
 }
 
 CgWork::~CgWork() {
@@ -339,6 +341,7 @@ int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,
   NB_CUDA(cudaMemcpy(op->fD, fDh.data(), lx * lx * sizeof(float), cudaMemcpyHostToDevice));
   // even-odd tables when D(n-1-i,n-1-m) = -D(i,m) holds to rounding
   op->eo_ok = even_odd_tables(op->D, lx, op->EO);
+  op->fx_ok = op->eo_ok && fx_tables(op->D, lx, op->FXhi, op->FXlo, &op->fx_fc);
   op->face.resize(nelt);
   for (int e = 0; e < nelt; ++e)
     op->face[e] = (unsigned char)face_bits(op->lglel[e], nelx, nely, nelz);
@@ -555,6 +558,7 @@ static int cg_begin_t(Operator &op, CgWork &wk, T *x, const T *f, const T *c,
   const long n = op.n;
   NB_TRY(wk.ensure(op, niter));
   wk.r32_ready = false;
+  if (std::is_same<T, double>::value) metric_fx_invalidate(op);
   if (zero_x) NB_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));  // rzero(x)
   NB_TRY(vec_copy<T>(r, f, n, s));                                 // copy(r,f)
   NB_TRY(maskit_dev<T>(op, r, s));

@@ -23,8 +23,21 @@ struct Operator {
   // even and D is anti-centrosymmetric to rounding
   std::vector<double> EO;
   bool eo_ok = false;
+  // the same tables in fixed point for the FP64 operator on the integer
+  // pipes (nb_ax_fx.cuh): balanced halves, fx_fc fractional bits
+  std::vector<int> FXhi, FXlo;
+  int fx_fc = 0;
+  bool fx_ok = false;
+  // the metric of the solve in progress in fixed point (metric_fx_prepare):
+  // balanced halves per value, one exponent per element, converted from
+  // gfx_src
+  mutable int2 *gfx = nullptr;
+  mutable int *gexp = nullptr;
+  mutable const double *gfx_src = nullptr;
+  mutable long gfx_cap = 0;
   int order = 1;                   // 0 reference left-to-right sums, 1 even-odd
-                                   // (FP64 and FP32 operators alike)
+                                   // (FP64 and FP32 operators alike), 2 the
+                                   // FP64 operator in fixed point (FP32: even-odd)
   GsHost gsh_host;                 // jl maps of the dssum handle
   GsDevice gs;                     // device form
   // mask state (maskit, cg.f:214-258)
@@ -88,6 +101,16 @@ int operator_from(Operator *op, int nelx, int nely, int nelz, int nelt,
 // E, O of D and of D^T (4*(lx/2)^2 values) when lx is even and D is
 // anti-centrosymmetric to rounding (the even-odd contraction form).
 bool even_odd_tables(const std::vector<double> &D, int lx, std::vector<double> &eo);
+// The even-odd tables in fixed point (nb_ax_fx.cu): balanced 32-bit halves of
+// round(C 2^fc), |round(C 2^fc)| <= 2^59, from D's exact values.
+bool fx_tables(const std::vector<double> &D, int lx, std::vector<int> &hi,
+               std::vector<int> &lo, int *fc);
+// The metric g in the fixed-point operator's form, converted when g is not
+// the array last converted (one pass over g); metric_fx_invalidate forgets
+// the conversion (every solve and every standalone apply starts with it, so
+// a caller may change g's contents between calls).
+int metric_fx_prepare(const Operator &op, const double *g, cudaStream_t s);
+void metric_fx_invalidate(const Operator &op);
 // The mesh-independent part of an operator: sizes, element numbers, D and
 // its even-odd tables, the domain faces of every element.
 int operator_base(Operator *op, int nelx, int nely, int nelz, int nelt, int lx,

@@ -781,6 +781,9 @@ orc_ctx *orc_ctx_new(int nelx, int nely, int nelz, int nelt, int nx1,
 
 static void mg_free(orc_mg *m);
 
+/* Threads of the OpenMP loops of later calls (1 = the scalar restatement). */
+void orc_ctx_set_threads(orc_ctx *c, int nthreads) { c->nthreads = nthreads > 0 ? nthreads : 1; }
+
 void orc_ctx_free(orc_ctx *c) {
   if (!c) return;
   orc_gs_free(c->gsh);

@@ -66,6 +66,7 @@ typedef struct orc_ctx orc_ctx;
 orc_ctx *orc_ctx_new(int nelx, int nely, int nelz, int nelt, int nx1,
                      const int *lglel, int mask_mode, int nthreads);
 void     orc_ctx_free(orc_ctx *c);
+void     orc_ctx_set_threads(orc_ctx *c, int nthreads);
 void     orc_ctx_reset_mask(orc_ctx *c);            /* init_mesh: cmask(-1)=1 */
 int      orc_ctx_n(const orc_ctx *c);
 const double *orc_ctx_dxm1(const orc_ctx *c);

@@ -14,10 +14,12 @@ set_multiplicity, proxy_setup, set_f, then cg twice (the warm-up and the timed
 call; the second one sees the reference's element-1 mask list, cg.f:214-258).
 Every glsc3 value the solver computes is recorded, in order.
 
-Run here, where the reference checkout exists:
+Run where the reference checkout exists (--ref <root>, else
+$NEKBONE_REFERENCE, else a checkout named "reference" beside this
+repository):
 
     make -C oracle all ref
-    python tests/golden/make_golden_fortran.py [--c1]
+    python tests/golden/make_golden_fortran.py [--ref <root>] [--c1]
 
 --c1 adds the C1 configuration (4^3 elements, lx1=10, 100 iterations per cg
 call, a few minutes).  Outputs: tests/golden/fortran_*.npz.
@@ -39,8 +41,18 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import f77  # noqa: E402
 from f77 import Ref  # noqa: E402
 
-REF = Path("/root/reference/src")
+REF = None  # the reference's src/ directory, set by main() from --ref
 JL = ROOT / "oracle" / "_ref" / "libjl_ref.so"
+
+
+def reference_src(arg: str | None) -> Path:
+    """src/ of the reference checkout: --ref, $NEKBONE_REFERENCE, or a
+    checkout named "reference" beside this repository."""
+    import os
+    root = Path(arg or os.environ.get("NEKBONE_REFERENCE") or ROOT.parent / "reference")
+    if not (root / "src" / "cg.f").exists():
+        raise SystemExit(f"no reference checkout at {root} (pass --ref or set NEKBONE_REFERENCE)")
+    return root / "src"
 
 
 # ------------------------------------------------------ external routines --
@@ -270,9 +282,10 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--c1", action="store_true", help="also the 4^3, lx1=10 C1 case")
     ap.add_argument("--only", choices=["speclib", "box", "hsmg", "c1"], default=None)
+    ap.add_argument("--ref", default=None, help="root of the reference checkout")
     a = ap.parse_args()
-    if not REF.exists():
-        sys.exit("the reference checkout is not present")
+    global REF
+    REF = reference_src(a.ref)
     if not JL.exists():
         sys.exit("build the jl library first: make -C oracle ref")
     gs = JlGs()

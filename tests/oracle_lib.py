@@ -40,7 +40,7 @@ def load(fma: bool = True) -> C.CDLL:
               "orc_set_f", "orc_dssum", "orc_maskit", "orc_ax", "orc_ax_local", "orc_ax_e",
               "orc_cg", "orc_h1mg_setup", "orc_h1mg_solve", "orc_h1mg_nlev", "orc_h1mg_order",
               "orc_h1mg_fdm_copy", "orc_ctx_n", "orc_flop_a", "orc_flop_cg",
-              "orc_ctx_dxm1", "orc_ctx_wxm1"):
+              "orc_ctx_dxm1", "orc_ctx_wxm1", "orc_ctx_set_threads"):
         getattr(L, f).argtypes = None
     _libs[key] = L
     return L
@@ -138,6 +138,9 @@ class Ctx:
     def wxm1(self):
         ptr = self.L.orc_ctx_wxm1(self.hv)
         return np.ctypeslib.as_array(ptr, shape=(self.nx1,)).copy()
+
+    def set_threads(self, nthreads: int) -> None:
+        self.L.orc_ctx_set_threads(self.hv, C.c_int(nthreads))
 
     def setup_g(self):
         g = np.zeros(6 * self.n)

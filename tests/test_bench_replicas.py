@@ -69,3 +69,38 @@ def test_reference_arm_runs_on_rank_zero_only():
     with contextlib.redirect_stdout(buf):
         bench.run_reference(a, rank=1, world=2)   # returns before touching a
     assert buf.getvalue() == ""
+
+
+def test_global_ids_match_set_vert_box():
+    """The bench's numpy global numbering is set_vert_box's (the oracle's
+    restatement of prox_dssum.f:42-73) on a brick box."""
+    sys.path.insert(0, str(ROOT))
+    sys.path.insert(0, str(ROOT / "tests"))
+    import numpy as np
+    import bench
+    import oracle_lib as O
+    for nel, lx in ((3, 5), (2, 12), (1, 2)):
+        nelt = nel ** 3
+        ref = O.set_vert_box(lx, nelt, nel, nel, nel, np.arange(1, nelt + 1))
+        assert np.array_equal(bench.global_ids(nel, lx), ref)
+
+
+def test_reference_arm_line_small_case():
+    """The reference arm on a small box prints one line with the workload
+    config our arm prints, the CPU baseline it measured and no copies."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class A:
+        pass
+    a = A()
+    a.nel, a.lx, a.niter, a.steps, a.warmup, a.cpu_sample_iters, a.gpus = 2, 6, 100, 2, 1, 3, 1
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        bench.run_reference(a, rank=0, world=1)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"] == bench.workload_config(2, 6, 100)
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["higher_is_better"] is True and line["unit"] == bench.UNIT

@@ -48,3 +48,32 @@ def test_glsc3_noalloc_rejects_sizes_beyond_its_scratch():
     assert status == 1
     assert b"outside" in nb.lib.nekbone_last_message()
     nb.lib.nekbone_clear_status()
+
+
+def test_glsc3_noalloc_empty_and_on_a_callers_stream():
+    """n = 0 writes 0.0 (its own path: no kernel); and a call enqueued on a
+    stream of the caller's, passed as its handle, gives glsc3_'s value once
+    that stream is synchronised."""
+    torch = pytest.importorskip("torch")
+    import nekbone_gb300 as nb
+
+    out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    assert nb.lib.nb_glsc3_noalloc(None, None, None, 0, out.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert out.item() == 0.0
+
+    rng = np.random.default_rng(31)
+    n = 1_000_003
+    a, b, m = rng.standard_normal(n), rng.standard_normal(n), rng.random(n)
+    expect = nb.glsc3(a, b, m)
+    ta, tb, tm = (torch.from_numpy(x).cuda() for x in (a, b, m))
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    out.fill_(float("nan"))
+    torch.cuda.synchronize()
+    status = nb.lib.nb_glsc3_noalloc(ta.data_ptr(), tb.data_ptr(), tm.data_ptr(), n,
+                                     out.data_ptr(), side.cuda_stream)
+    assert status == 0, nb.lib.nekbone_last_message()
+    side.synchronize()
+    assert abs(out.item() - expect) <= 1e-12 * float(np.sum(np.abs(a * b * m)))
