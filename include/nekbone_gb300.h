@@ -56,11 +56,15 @@ void nekbone_set_mask_mode_(const int *mode);
 /* .true. selects h1mg_solve as solveM (MGRID build, cg.f:86-94,
  * hsmg.f:960); .false. the copy of hsmg_dum.f:9-14. */
 void nekbone_set_mgrid_(const int *ifmgrid);
-/* Summation order of the FP64 element contractions: 0 = the reference's
- * left-to-right mxm sums (mxm_std.f:255; bit-identical to a left-to-right
- * fma evaluation), 1 = even-odd split of the anti-centrosymmetric GLL
- * derivative (default; same result to rounding, ~27% fewer FP64 operations).
- * ax_e_ always uses order 0. */
+/* Form of the FP64 element operator: 0 = the reference's left-to-right mxm
+ * sums (mxm_std.f:255; bit-identical to a left-to-right fma evaluation),
+ * 1 = even-odd split of the anti-centrosymmetric GLL derivative on the FP64
+ * pipe (same result to rounding, ~27% fewer FP64 operations), 2 = the
+ * even-odd form in 64-bit fixed point on the integer pipes (default: block
+ * floating point, ~58 significant bits of each element's largest value;
+ * same result to rounding, ~3x faster on GB300, whose FP64 pipe runs at
+ * 1/64 of its FP32 rate).  Odd lx1 falls back to order 0; ax_e_ always uses
+ * order 0. */
 void nekbone_set_contraction_order_(const int *order);
 /* /cflops/ flop_a, flop_cg (INPUT:8), accumulated as the reference does */
 void nekbone_get_flops_(double *flop_a, double *flop_cg);

@@ -27,6 +27,9 @@ if not _LIB_PATH.exists():
 
 lib = _C.CDLL(str(_LIB_PATH))
 
+#: the library's default FP64 operator form (nekbone_set_contraction_order_)
+DEFAULT_ORDER = 2
+
 _i = _C.c_int
 _l = _C.c_long
 _d = _C.c_double
@@ -349,7 +352,8 @@ class Nekbone:
 
     @staticmethod
     def set_order(order: int) -> None:
-        """0 = reference left-to-right contraction sums, 1 = even-odd split."""
+        """0 = reference left-to-right contraction sums, 1 = even-odd split
+        on the FP64 pipe, 2 = even-odd in 64-bit fixed point (DEFAULT_ORDER)."""
         lib.nekbone_set_contraction_order_(_ref(order))
         _check()
 

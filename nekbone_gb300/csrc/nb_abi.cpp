@@ -116,7 +116,7 @@ struct State {
   std::vector<int> lglel;
   std::vector<double> dxm1;
   int mask_mode = 0;
-  int order = 1;  // contraction order of the FP64 operator (1 even-odd)
+  int order = 2;  // contraction form of the FP64 operator (2 fixed point)
   bool mgrid = false;
   double flop_a = 0.0, flop_cg = 0.0;
   std::unique_ptr<Operator> op;

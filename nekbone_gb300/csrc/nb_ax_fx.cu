@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 // E, O of D and of D^T (even_odd_tables' order and meaning) in fixed point
-// with fc fractional bits, |C| <= 2^58, split into balanced halves.
+// with fc fractional bits, |C| <= 2^59, split into balanced halves.
 bool fx_tables(const std::vector<double> &D, int lx, std::vector<int> &hi,
                std::vector<int> &lo, int *fc) {
   if (lx % 2 != 0 || lx < 2) return false;
@@ -92,7 +92,7 @@ bool fx_tables(const std::vector<double> &D, int lx, std::vector<int> &hi,
   if (!(mx > 0.0)) return false;
   int k = 0;
   std::frexp(mx * (1.0 + 1e-15), &k);  // mx < 2^k
-  *fc = 58 - k;
+  *fc = 59 - k;
   hi.assign(4 * h * h, 0);
   lo.assign(4 * h * h, 0);
   auto put = [&](int q, double x1, double x2, int sgn) {

@@ -13,7 +13,7 @@
 //  * each element's input p is scaled by one power of two chosen from the
 //    element's largest exponent and rounded to an integer P, |P| < 2^59
 //    (to_fixed); the derivative tables are fixed-point integers with FC
-//    fractional bits (|C| <= 2^58, rounded once on the host from D's exact
+//    fractional bits (|C| <= 2^59, rounded once on the host from D's exact
 //    value); the metric g is converted once per solve, one exponent per
 //    element (|G| < 2^60);
 //  * a product a*b of two such integers is formed from balanced 32-bit
@@ -21,12 +21,10 @@
 //        a*b ~= ah*bh 2^64 + (ah*bl + al*bh) 2^32,
 //    al*bl (|al*bl| <= 2^62, unbiased: al is symmetric) dropped; the terms
 //    of one output are accumulated in two int64 registers (Acc) and
-//    combined once, rounded to units of 2^60 (2^62 for the transposed
-//    gradient, whose three outputs are summed in int64: each is below
-//    2^59.6; 2^64 for the metric step), so one output's error is a few
-//    units, ~2^-57 of its largest product.  The rounding costs nothing (the
-//    accumulator starts at half a unit) and neither does the scaling (the hi
-//    halves of the coefficients come pre-scaled);
+//    combined once, rounded to units of 2^64 (hh + x / 2^32: the high word
+//    of x, no shift), so one output's error is about one unit, ~2^-55 of its
+//    largest product -- the FP64 evaluation's own rounding of a 6-term sum.
+//    The rounding costs nothing: x starts at half a unit;
 //  * the even-odd split of the GLL derivative (as k_ax_eo) halves the
 //    products: per point and direction 6 multiply-adds at lx1 = 12;
 //  * after the gradient and after the metric step the element's values are
@@ -47,6 +45,11 @@
 
 #include "nb_kernels.cuh"
 
+// CTAs per SM the fixed-point operator asks registers for at lx1 <= 12
+#ifndef NB_FX_MINB
+#define NB_FX_MINB 4
+#endif
+
 namespace nb {
 namespace fx {
 
@@ -66,23 +69,27 @@ __device__ __forceinline__ Sp split(i64 x) {
   return s;
 }
 
-// A sum of products a*b in units of 2^U: hh counts ah*bh 2^(64-U) -- the
-// caller passes ah already scaled by 2^(64-U) (chs) -- and x counts
-// (ah*bl + al*bh) in units of 2^32, started at half a unit of 2^U so that the
-// final shift rounds to nearest (al*bl dropped).
-template <int U>
+// A sum of products a*b in units of 2^64: hh counts ah*bh, x counts
+// (ah*bl + al*bh) in units of 2^32, started at half a unit so that taking
+// its high word rounds to nearest (al*bl dropped).  Each product is one
+// 32x32 -> 64-bit multiply-add (mad.wide.s32), written in C++ so that a
+// coefficient stays an immediate constant-bank operand.
 struct Acc {
   i64 hh, x;
-  __device__ __forceinline__ Acc() : hh(0), x(1ll << (U - 33)) {}
-  __device__ __forceinline__ void mac(int chs, int chi, int clo, const Sp &v) {
-    hh += i64(chs) * i64(v.hi);
+  __device__ __forceinline__ Acc() : hh(0), x(1ll << 31) {}
+  __device__ __forceinline__ void mac(int chi, int clo, const Sp &v) {
+    hh += i64(chi) * i64(v.hi);
     x += i64(chi) * i64(v.lo);
     x += i64(clo) * i64(v.hi);
   }
-  __device__ __forceinline__ i64 result() const { return hh + (x >> (U - 32)); }
+  __device__ __forceinline__ void mac(const Sp &c, const Sp &v) { mac(c.hi, c.lo, v); }
+  __device__ __forceinline__ i64 result() const { return hh + (x >> 32); }
 };
 
-// v * 2^sh, rounded to nearest for sh < 0
+// v * 2^sh, rounded to nearest for sh < 0 (sh is the same in the whole
+// block: a renormalisation shift).  A separate fast path for 0 <= sh < 32
+// measured 1 ms slower at 32^3: the branch in every unrolled load keeps the
+// compiler from scheduling the loads.
 __device__ __forceinline__ i64 shift_signed(i64 v, int sh) {
   return sh >= 0 ? i64(u64(v) << sh) : ((v + (1ll << (-sh - 1))) >> (-sh));
 }
@@ -142,19 +149,14 @@ __device__ __forceinline__ unsigned warp_mask(int nt, int w) {
 }
 
 // ------------------------------------------------------------ operator --
-// Units of the contraction outputs: the gradient's 2^60, the transposed
-// gradient's 2^62 (its three outputs are summed in int64).
-constexpr int kUGrad = 60, kUGradT = 62;
-
 // Derivative tables in fixed point: E, O of D, then E, O of D^T (the
 // even-odd tables of k_ax_eo, 4*(lx1/2)^2 values, row a), as balanced
-// halves, |coefficient| <= 2^58; hs = hi scaled by 2^(64 - U) of the stage
-// that uses the table.  A kernel parameter, read as multiply-add operands.
+// halves, |coefficient| <= 2^59.  A kernel parameter, read as multiply-add
+// operands.
 template <int LX>
 struct FxCoef {
   int hi[4 * (LX / 2) * (LX / 2)];
   int lo[4 * (LX / 2) * (LX / 2)];
-  int hs[4 * (LX / 2) * (LX / 2)];
   int fc;  // fractional bits: coefficient = (hi 2^32 + lo) 2^-fc
 };
 
@@ -175,10 +177,11 @@ __device__ __forceinline__ int fx_at(int i, int j, int k) {
 }
 
 // y(0..n-1) = C v of one line v (fixed point, |v| < 2^59), coefficient
-// tables at offset q0 of cf (E at q0, O at q0 + h^2); y in units of 2^U of
-// the products (|y| < 2^(120.6 - U))
-template <int LX, int U>
-__device__ __forceinline__ void fx_line(const i64 *v, const FxCoef<LX> &cf, int q0, i64 *y) {
+// tables at offset q0 of cf (E at q0, O at q0 + h^2); y in units of 2^64 of
+// the products (|y| < 2^58.6), handed to put(m, y(m)) as soon as each pair
+// y(a), y(n-1-a) is formed (no output array stays live)
+template <int LX, typename Put>
+__device__ __forceinline__ void fx_line(const i64 *v, const FxCoef<LX> &cf, int q0, Put put) {
   constexpr int H = LX / 2;
   Sp ve[H], vo[H];
 #pragma unroll
@@ -188,16 +191,16 @@ __device__ __forceinline__ void fx_line(const i64 *v, const FxCoef<LX> &cf, int 
   }
 #pragma unroll
   for (int a = 0; a < H; ++a) {
-    Acc<U> e, o;
+    Acc e, o;
 #pragma unroll
     for (int m = 0; m < H; ++m) {
       const int qe = q0 + a * H + m, qo = qe + H * H;
-      e.mac(cf.hs[qe], cf.hi[qe], cf.lo[qe], ve[m]);
-      o.mac(cf.hs[qo], cf.hi[qo], cf.lo[qo], vo[m]);
+      e.mac(cf.hi[qe], cf.lo[qe], ve[m]);
+      o.mac(cf.hi[qo], cf.lo[qo], vo[m]);
     }
     const i64 ye = e.result(), yo = o.result();
-    y[a] = ye + yo;
-    y[LX - 1 - a] = yo - ye;
+    put(a, ye + yo);
+    put(LX - 1 - a, yo - ye);
   }
 }
 
@@ -287,33 +290,30 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   u64 orv = 0;
   i64 col[LX];
   {
-    i64 v[LX], y[LX];
+    i64 v[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(m, i, j)];  // r-line
-    fx_line<LX, kUGrad>(v, cf, 0, y);
-#pragma unroll
-    for (int m = 0; m < LX; ++m) {
-      sm.B[fx_at<LX>(m, i, j)] = y[m];
-      orv |= mag(y[m]);
-    }
+    fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
+      sm.B[fx_at<LX>(m, i, j)] = y;
+      orv |= mag(y);
+    });
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, m, j)];  // s-line
-    fx_line<LX, kUGrad>(v, cf, 0, y);
-#pragma unroll
-    for (int m = 0; m < LX; ++m) {
-      sm.C[fx_at<LX>(i, m, j)] = y[m];
-      orv |= mag(y[m]);
-    }
+    fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
+      sm.C[fx_at<LX>(i, m, j)] = y;
+      orv |= mag(y);
+    });
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, j, m)];  // t-line
-    fx_line<LX, kUGrad>(v, cf, 0, col);
-#pragma unroll
-    for (int m = 0; m < LX; ++m) orv |= mag(col[m]);
+    fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
+      col[m] = y;
+      orv |= mag(y);
+    });
   }
   fx_or_post(orv, sm.orl, sm.orh, t, L2);
   __syncthreads();
   const int s1 = fx_or_shift(sm.orl, sm.orh, L2);
-  const int sU = sP - fc + kUGrad - s1;  // ur = UR 2^sU after the shift
+  const int sU = sP - fc + 64 - s1;  // ur = UR 2^sU after the shift
 
   // metric (cg.f:156-163) at the thread's own points: G (balanced halves)
   // times the gradient, products in units of 2^64
@@ -329,10 +329,10 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
     const int4 g01 = __ldg(gp), g23 = __ldg(gp + 1), g45 = __ldg(gp + 2);
     const Sp G1 = {g01.x, g01.y}, G2 = {g01.z, g01.w}, G3 = {g23.x, g23.y},
              G4 = {g23.z, g23.w}, G5 = {g45.x, g45.y}, G6 = {g45.z, g45.w};
-    Acc<64> wr, ws, wt;
-    wr.mac(G1.hi, G1.hi, G1.lo, ur); wr.mac(G2.hi, G2.hi, G2.lo, us); wr.mac(G3.hi, G3.hi, G3.lo, ut);
-    ws.mac(G2.hi, G2.hi, G2.lo, ur); ws.mac(G4.hi, G4.hi, G4.lo, us); ws.mac(G5.hi, G5.hi, G5.lo, ut);
-    wt.mac(G3.hi, G3.hi, G3.lo, ur); wt.mac(G5.hi, G5.hi, G5.lo, us); wt.mac(G6.hi, G6.hi, G6.lo, ut);
+    Acc wr, ws, wt;
+    wr.mac(G1, ur); wr.mac(G2, us); wr.mac(G3, ut);
+    ws.mac(G2, ur); ws.mac(G4, us); ws.mac(G5, ut);
+    wt.mac(G3, ur); wt.mac(G5, us); wt.mac(G6, ut);
     const i64 r_ = wr.result(), s_ = ws.result(), t_ = wt.result();
     sm.B[q] = r_;
     sm.C[q] = s_;
@@ -342,32 +342,25 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   fx_or_post(orv, sm.orl, sm.orh, t, L2);
   __syncthreads();
   const int s2 = fx_or_shift(sm.orl, sm.orh, L2);
-  const int sT = kUGradT - fc + sW - s2;  // transposed-gradient outputs: value 2^sT
+  const int sT = 64 - fc + sW - s2;  // transposed-gradient outputs: value 2^sT
 
   // transposed gradient (local_grad3_t) with D^T: tr into A, ts into B
   // (after every r-line of B was read), tt in registers
   {
-    i64 v[LX], y[LX];
+    i64 v[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.B[fx_at<LX>(m, i, j)], s2);
-    fx_line<LX, kUGradT>(v, cf, 2 * H * H, y);
-#pragma unroll
-    for (int m = 0; m < LX; ++m) sm.A[fx_at<LX>(m, i, j)] = y[m];  // tr
+    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { sm.A[fx_at<LX>(m, i, j)] = y; });  // tr
   }
   __syncthreads();
   {
-    i64 v[LX], y[LX];
-#pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.C[fx_at<LX>(i, m, j)], s2);
-    fx_line<LX, kUGradT>(v, cf, 2 * H * H, y);
-#pragma unroll
-    for (int m = 0; m < LX; ++m) sm.B[fx_at<LX>(i, m, j)] = y[m];  // ts
-  }
-  {
     i64 v[LX];
 #pragma unroll
+    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.C[fx_at<LX>(i, m, j)], s2);
+    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { sm.B[fx_at<LX>(i, m, j)] = y; });  // ts
+#pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = shift_signed(col[m], s2);
-    fx_line<LX, kUGradT>(v, cf, 2 * H * H, col);  // tt
+    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { col[m] = y; });  // tt
   }
   __syncthreads();
 
@@ -417,7 +410,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
 }
 
 template <int LX, int MODE>
-__global__ void __launch_bounds__(LX * LX, (LX <= 12 ? 4 : 1))
+__global__ void __launch_bounds__(LX * LX, (LX <= 12 ? NB_FX_MINB : 1))
     k_ax_fx(AxArgs<double> a, const __grid_constant__ FxCoef<LX> cf) {
   ax_fx_body<LX, MODE>(a, cf);
 }

@@ -23,8 +23,6 @@ int launch_ax_fx_shape(const Operator &op, AxArgs<double> a, cudaStream_t s) {
   for (int q = 0; q < Q; ++q) {
     cf.hi[q] = op.FXhi[q];
     cf.lo[q] = op.FXlo[q];
-    // the gradient's tables (D) at units 2^60, the transposed ones at 2^62
-    cf.hs[q] = op.FXhi[q] * (q < Q / 2 ? (1 << (64 - fx::kUGrad)) : (1 << (64 - fx::kUGradT)));
   }
   cf.fc = op.fx_fc;
   fx::k_ax_fx<LX, MODE><<<a.nelt, dim3(LX, LX), sm, s>>>(a, cf);

@@ -35,9 +35,10 @@ struct Operator {
   mutable int *gexp = nullptr;
   mutable const double *gfx_src = nullptr;
   mutable long gfx_cap = 0;
-  int order = 1;                   // 0 reference left-to-right sums, 1 even-odd
-                                   // (FP64 and FP32 operators alike), 2 the
-                                   // FP64 operator in fixed point (FP32: even-odd)
+  int order = 2;                   // 0 reference left-to-right sums, 1 even-odd
+                                   // (FP64 and FP32 operators alike), 2 (default)
+                                   // the FP64 operator in fixed point where the
+                                   // even-odd tables exist (FP32: even-odd)
   GsHost gsh_host;                 // jl maps of the dssum handle
   GsDevice gs;                     // device form
   // mask state (maskit, cg.f:214-258)

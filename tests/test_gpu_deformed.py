@@ -89,7 +89,7 @@ def test_fp32_operator_error_vs_fp64_oracle(torch, lx):
     m.ax(w.data_ptr(), ut.data_ptr(), g.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(w.cpu().numpy(), w64)
-    m.set_order(1)
+    m.set_order(nb.DEFAULT_ORDER)
     # FP32 operator
     w32 = torch.empty(m.n, dtype=torch.float32, device="cuda")
     u32, g32 = ut.float(), g.float()

@@ -83,7 +83,7 @@ def test_headline_kernels_device_api_match_oracle(nb, device_case, order):
         x, r, w, p, z = vs
         hist = m.cg(*(t.data_ptr() for t in (x, f, g, c, r, w, p, z)), NITER, hist=True)
     finally:
-        m.set_order(1)
+        m.set_order(nb.DEFAULT_ORDER)
     scale = float(f.abs().max())
     assert rel(x.cpu().numpy(), o["x"]) < 1e-12
     for name, a in (("r", r), ("p", p), ("w", w)):
@@ -108,7 +108,7 @@ def test_headline_kernels_dropin_cg_match_oracle(nb, order):
         work = tuple(np.zeros(mesh.n) for _ in range(5))
         x, r, w, p, z, _ = mesh.cg(f, g, c, NITER, 0.0, work)
     finally:
-        nb.Nekbone.set_order(1)
+        nb.Nekbone.set_order(nb.DEFAULT_ORDER)
     o = ctx.cg(f, g, c, NITER)
     scale = np.max(np.abs(f))
     assert rel(x, o["x"]) < 1e-12
@@ -142,7 +142,7 @@ def test_ax_fixed_point_matches_oracle(nb, dims, mask_mode):
             got = mesh.ax(u, g)
             assert np.max(np.abs(got - ref)) <= 1e-13 * np.max(np.abs(ref)) + 1e-320, tiny
     finally:
-        nb.Nekbone.set_order(1)
+        nb.Nekbone.set_order(nb.DEFAULT_ORDER)
 
 
 @pytest.mark.parametrize("order", [0, 1, 2])
@@ -175,7 +175,7 @@ def test_deformed_cg_matches_oracle(nb, order):
         hist = m.cg(*(t.data_ptr() for t in (vs[0], f, g, c, vs[1], vs[2], vs[3], vs[4])), 60,
                     hist=True)
     finally:
-        m.set_order(1)
+        m.set_order(nb.DEFAULT_ORDER)
     assert rel(vs[0].cpu().numpy(), o["x"]) < 1e-11
     assert np.allclose(hist[:, 0], o["hist"][:, 0], rtol=1e-10, atol=0)
     m.close()
@@ -207,7 +207,7 @@ def test_fixed_point_metric_reconverted_between_solves(nb):
             o = ctx.cg(f.cpu().numpy(), g.cpu().numpy(), c.cpu().numpy(), 30)
             assert rel(vs[0].cpu().numpy(), o["x"]) < 1e-12, deformed
     finally:
-        m.set_order(1)
+        m.set_order(nb.DEFAULT_ORDER)
     m.close()
 
 
@@ -233,7 +233,7 @@ def test_mixed_defect_correction_residual_against_oracle(nb, order):
         outer, inner, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
                                       1e-10, 20)
     finally:
-        m.set_order(1)
+        m.set_order(nb.DEFAULT_ORDER)
     assert rr <= 1e-10
     ctx = O.Ctx(*dims, mask_mode=1)
     fh, ch = f.cpu().numpy(), c.cpu().numpy()

@@ -52,7 +52,7 @@ def test_mg_explicit_levels_match_oracle(torch):
     torch.cuda.synchronize()
     zo = ctx.h1mg_solve(f.cpu().numpy().copy())
     zg = z.cpu().numpy()
-    assert np.max(np.abs(zg - zo)) <= 1e-10 * np.max(np.abs(zo))
+    assert np.max(np.abs(zg - zo)) <= 1e-12 * np.max(np.abs(zo))
 
 
 def test_fp32_smoother_close_to_fp64(torch):
