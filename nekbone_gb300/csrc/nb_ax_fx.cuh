@@ -45,10 +45,18 @@
 
 #include "nb_kernels.cuh"
 
-// CTAs per SM the fixed-point operator asks registers for at lx1 <= 12
+// CTAs per SM of the fixed-point operator at lx1 <= 12 (its four
+// shared-memory arrays, 60 KB at lx1 = 12, allow three); the output rows of a
+// line are unrolled two at a time (fully unrolled, the kernel spills and
+// measures slower)
 #ifndef NB_FX_MINB
-#define NB_FX_MINB 4
+#define NB_FX_MINB 3
 #endif
+#ifndef NB_FX_AUNROLL
+#define NB_FX_AUNROLL 2
+#endif
+#define NB_FX_PRAGMA(x) _Pragma(#x)
+#define NB_FX_UNROLL(n) NB_FX_PRAGMA(unroll n)
 
 namespace nb {
 namespace fx {
@@ -69,21 +77,22 @@ __device__ __forceinline__ Sp split(i64 x) {
   return s;
 }
 
-// A sum of products a*b in units of 2^64: hh counts ah*bh, x counts
-// (ah*bl + al*bh) in units of 2^32, started at half a unit so that taking
-// its high word rounds to nearest (al*bl dropped).  Each product is one
-// 32x32 -> 64-bit multiply-add (mad.wide.s32), written in C++ so that a
-// coefficient stays an immediate constant-bank operand.
+// A sum of products a*b in units of 2^64: hh counts ah*bh, x and x2 count
+// ah*bl and al*bh in units of 2^32 (two accumulators: two dependency chains
+// of half the length), x started at half a unit so that the high word of
+// x + x2 rounds to nearest (al*bl dropped).  Each product is one 32x32 ->
+// 64-bit multiply-add (mad.wide.s32), written in C++ so that a coefficient
+// can stay a constant-bank operand.
 struct Acc {
-  i64 hh, x;
-  __device__ __forceinline__ Acc() : hh(0), x(1ll << 31) {}
+  i64 hh, x, x2;
+  __device__ __forceinline__ Acc() : hh(0), x(1ll << 31), x2(0) {}
   __device__ __forceinline__ void mac(int chi, int clo, const Sp &v) {
     hh += i64(chi) * i64(v.hi);
     x += i64(chi) * i64(v.lo);
-    x += i64(clo) * i64(v.hi);
+    x2 += i64(clo) * i64(v.hi);
   }
   __device__ __forceinline__ void mac(const Sp &c, const Sp &v) { mac(c.hi, c.lo, v); }
-  __device__ __forceinline__ i64 result() const { return hh + (x >> 32); }
+  __device__ __forceinline__ i64 result() const { return hh + ((x + x2) >> 32); }
 };
 
 // v * 2^sh, rounded to nearest for sh < 0 (sh is the same in the whole
@@ -166,6 +175,7 @@ struct FxShared {
   i64 A[N];
   i64 B[N];
   i64 C[N];
+  i64 D[N];
   int emax[8];
   unsigned orl[8], orh[8];
   double red[32];
@@ -189,7 +199,7 @@ __device__ __forceinline__ void fx_line(const i64 *v, const FxCoef<LX> &cf, int 
     ve[m] = split(v[m] + v[LX - 1 - m]);
     vo[m] = split(v[m] - v[LX - 1 - m]);
   }
-#pragma unroll
+  NB_FX_UNROLL(NB_FX_AUNROLL)
   for (int a = 0; a < H; ++a) {
     Acc e, o;
 #pragma unroll
@@ -284,29 +294,24 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int sP = em - 1081;  // p = P 2^sP
   __syncthreads();
 
-  // gradient (local_grad3): thread (i,j) takes the r-line (j=i, k=j) and the
-  // s-line (i, k=j) (consecutive threads on distinct banks), from A into B
-  // and C, and its own column, the t-line (i,j), into registers
+  // Thread (i,j) takes, in each contraction stage, the r-line (j=i, k=j),
+  // the s-line (i, k=j) and its own column, the t-line (i,j): one loop over
+  // the three directions with run-time strides keeps one copy of the line
+  // code per stage; every output goes to shared memory.
+  const int lb0 = fx_at<LX>(0, i, j), lb1 = fx_at<LX>(i, 0, j), lb2 = fx_at<LX>(i, j, 0);
+
+  // gradient (local_grad3): A -> B (ur), C (us), D (ut)
   u64 orv = 0;
-  i64 col[LX];
-  {
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
+    const int st = d == 0 ? 1 : d == 1 ? LX + 1 : (LX + 1) * LX;
+    i64 *out = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
     i64 v[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(m, i, j)];  // r-line
+    for (int m = 0; m < LX; ++m) v[m] = sm.A[b0 + m * st];
     fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
-      sm.B[fx_at<LX>(m, i, j)] = y;
-      orv |= mag(y);
-    });
-#pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, m, j)];  // s-line
-    fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
-      sm.C[fx_at<LX>(i, m, j)] = y;
-      orv |= mag(y);
-    });
-#pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = sm.A[fx_at<LX>(i, j, m)];  // t-line
-    fx_line<LX>(v, cf, 0, [&](int m, i64 y) {
-      col[m] = y;
+      out[b0 + m * st] = y;
       orv |= mag(y);
     });
   }
@@ -315,16 +320,15 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int s1 = fx_or_shift(sm.orl, sm.orh, L2);
   const int sU = sP - fc + 64 - s1;  // ur = UR 2^sU after the shift
 
-  // metric (cg.f:156-163) at the thread's own points: G (balanced halves)
-  // times the gradient, products in units of 2^64
+  // metric (cg.f:156-163) at the thread's own points, in place
   const int eg = a.gexp[e];
   const int sW = 64 + (eg - 1082) + sU;  // wr = WR 2^sW before renormalising
   orv = 0;
-#pragma unroll
+#pragma unroll 2
   for (int k = 0; k < LX; ++k) {
     const int q = fx_at<LX>(i, j, k);
     const Sp ur = split(shift_signed(sm.B[q], s1)), us = split(shift_signed(sm.C[q], s1)),
-             ut = split(shift_signed(col[k], s1));
+             ut = split(shift_signed(sm.D[q], s1));
     const int4 *gp = reinterpret_cast<const int4 *>(a.gfx + 6 * (base + size_t(k) * L2 + t));
     const int4 g01 = __ldg(gp), g23 = __ldg(gp + 1), g45 = __ldg(gp + 2);
     const Sp G1 = {g01.x, g01.y}, G2 = {g01.z, g01.w}, G3 = {g23.x, g23.y},
@@ -336,7 +340,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
     const i64 r_ = wr.result(), s_ = ws.result(), t_ = wt.result();
     sm.B[q] = r_;
     sm.C[q] = s_;
-    col[k] = t_;
+    sm.D[q] = t_;
     orv |= mag(r_) | mag(s_) | mag(t_);
   }
   fx_or_post(orv, sm.orl, sm.orh, t, L2);
@@ -344,23 +348,20 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int s2 = fx_or_shift(sm.orl, sm.orh, L2);
   const int sT = 64 - fc + sW - s2;  // transposed-gradient outputs: value 2^sT
 
-  // transposed gradient (local_grad3_t) with D^T: tr into A, ts into B
-  // (after every r-line of B was read), tt in registers
-  {
+  // transposed gradient (local_grad3_t) with D^T: B -> A (tr); after every
+  // r-line of B was read, C -> B (ts); D -> D (tt: the own column, read and
+  // written by this thread alone)
+#pragma unroll 1
+  for (int d = 0; d < 3; ++d) {
+    const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
+    const int st = d == 0 ? 1 : d == 1 ? LX + 1 : (LX + 1) * LX;
+    const i64 *src = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
+    i64 *out = d == 0 ? sm.A : d == 1 ? sm.B : sm.D;
     i64 v[LX];
 #pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.B[fx_at<LX>(m, i, j)], s2);
-    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { sm.A[fx_at<LX>(m, i, j)] = y; });  // tr
-  }
-  __syncthreads();
-  {
-    i64 v[LX];
-#pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = shift_signed(sm.C[fx_at<LX>(i, m, j)], s2);
-    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { sm.B[fx_at<LX>(i, m, j)] = y; });  // ts
-#pragma unroll
-    for (int m = 0; m < LX; ++m) v[m] = shift_signed(col[m], s2);
-    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { col[m] = y; });  // tt
+    for (int m = 0; m < LX; ++m) v[m] = shift_signed(src[b0 + m * st], s2);
+    if (d == 1) __syncthreads();
+    fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { out[b0 + m * st] = y; });
   }
   __syncthreads();
 
@@ -382,7 +383,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = fx_at<LX>(i, j, k);
-    double wl = to_double(sm.A[q] + sm.B[q] + col[k], sT);
+    double wl = to_double(sm.A[q] + sm.B[q] + sm.D[q], sT);
     const size_t id = base + size_t(k) * L2 + t;
     const bool interior = col_interior && (k > 0) && (k < LX - 1);
     if (MODE == 1) {
