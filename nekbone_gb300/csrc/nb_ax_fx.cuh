@@ -46,11 +46,12 @@
 #include "nb_kernels.cuh"
 
 // CTAs per SM of the fixed-point operator at lx1 <= 12 (its four
-// shared-memory arrays, 60 KB at lx1 = 12, allow three); the output rows of a
-// line are unrolled two at a time (fully unrolled, the kernel spills and
-// measures slower)
+// shared-memory arrays, 56 KB at lx1 = 12, allow four: 2.01 ms at 32^3
+// against 2.25 ms with rows padded to lx1 + 1 and three CTAs); the output
+// rows of a line are unrolled two at a time (fully unrolled, the kernel
+// spills and measures slower)
 #ifndef NB_FX_MINB
-#define NB_FX_MINB 3
+#define NB_FX_MINB 4
 #endif
 #ifndef NB_FX_AUNROLL
 #define NB_FX_AUNROLL 2
@@ -171,7 +172,7 @@ struct FxCoef {
 
 template <int LX>
 struct FxShared {
-  static constexpr int N = (LX + 1) * LX * LX;
+  static constexpr int N = (LX * LX + 1) * LX;
   i64 A[N];
   i64 B[N];
   i64 C[N];
@@ -181,9 +182,13 @@ struct FxShared {
   double red[32];
 };
 
+// Element arrays in shared memory: rows of lx1 8-byte words, planes lx1^2 + 1
+// words apart.  The plane pitch is 1 modulo 16, so the r-lines that 16
+// consecutive threads start (thread t: j = t / lx1, k = t mod lx1) fall on
+// distinct banks; so do the own columns (i + lx1 j).
 template <int LX>
 __device__ __forceinline__ int fx_at(int i, int j, int k) {
-  return i + (LX + 1) * j + (LX + 1) * LX * k;
+  return i + LX * j + (LX * LX + 1) * k;
 }
 
 // y(0..n-1) = C v of one line v (fixed point, |v| < 2^59), coefficient
@@ -294,18 +299,18 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int sP = em - 1081;  // p = P 2^sP
   __syncthreads();
 
-  // Thread (i,j) takes, in each contraction stage, the r-line (j=i, k=j),
+  // Thread (i,j) takes, in each contraction stage, the r-line (j, k=i),
   // the s-line (i, k=j) and its own column, the t-line (i,j): one loop over
   // the three directions with run-time strides keeps one copy of the line
   // code per stage; every output goes to shared memory.
-  const int lb0 = fx_at<LX>(0, i, j), lb1 = fx_at<LX>(i, 0, j), lb2 = fx_at<LX>(i, j, 0);
+  const int lb0 = fx_at<LX>(0, j, i), lb1 = fx_at<LX>(i, 0, j), lb2 = fx_at<LX>(i, j, 0);
 
   // gradient (local_grad3): A -> B (ur), C (us), D (ut)
   u64 orv = 0;
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
-    const int st = d == 0 ? 1 : d == 1 ? LX + 1 : (LX + 1) * LX;
+    const int st = d == 0 ? 1 : d == 1 ? LX : (LX * LX + 1);
     i64 *out = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
     i64 v[LX];
 #pragma unroll
@@ -354,7 +359,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
-    const int st = d == 0 ? 1 : d == 1 ? LX + 1 : (LX + 1) * LX;
+    const int st = d == 0 ? 1 : d == 1 ? LX : (LX * LX + 1);
     const i64 *src = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
     i64 *out = d == 0 ? sm.A : d == 1 ? sm.B : sm.D;
     i64 v[LX];
