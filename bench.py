@@ -442,6 +442,9 @@ def batched(nb, torch, dev, reps=3):
         b.x_out(xh.data_ptr())
         nb.sync()
     e2e_ms = (time.perf_counter() - t0) / reps * 1e3
+    # per-phase device times of one solve, launched cycle by cycle with an
+    # event after every kernel (the graph solve runs them without the events)
+    phases, _ = b.time_phases(1e-10, INNER_MAX, 60)
     lxs = sorted({bx[3] for bx in boxes})
     out = {
         "workload": "256 box problems, elements log-uniform in [8,4096] (cubic factorisation), "
@@ -455,6 +458,8 @@ def batched(nb, torch, dev, reps=3):
         "min_outer": min(r[0] for r in res),
         "inner_gdof_iter_per_s": work / (ms * 1e-3) / 1e9,
         "e2e_ms": e2e_ms, "e2e_h2d_bytes": 8 * b.n, "e2e_d2h_bytes": 8 * b.n,
+        "phase_ms": {k: round(v, 4) for k, v in phases.items()},
+        "phase_ms_sum": round(sum(phases.values()), 4),
     }
     b.close()
     return out

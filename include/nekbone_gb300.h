@@ -384,6 +384,17 @@ int nb_batch_set_tuning(nb_batch *batch, int lx1, int epb32, int rd32, int epb64
  * inner_iters FP32 CG iterations, at most max_outer cycles) as one graph
  * launch on the library stream; x starts at 0. */
 int nb_batch_solve(nb_batch *batch, double tol, int inner_iters, int max_outer);
+/* Diagnostic: the same solve, same kernels and same results, launched one
+ * cycle at a time (each cycle a graph with an event after every launch, the
+ * loop condition read on the host between cycles), and synchronous.  ms[7]
+ * gets each phase's device time summed over the solve: 0 initial norms,
+ * 1 cycle start (scale r into the FP32 right-hand side), 2 inner element
+ * operator, 3 inner gather-scatter and p'Ap, 4 inner x/r/p update, 5 FP64
+ * defect element operator, 6 defect gather-scatter and residual norm;
+ * cycles gets the cycles run.  The loop-condition kernel of the graph solve
+ * (one block per cycle) is not part of it. */
+int nb_batch_time_phases(nb_batch *batch, double tol, int inner_iters, int max_outer,
+                         double *ms, int *cycles);
 /* Inner stopping of later solves: 0 (default) every cycle runs inner_iters
  * FP32 iterations; itol in (0, 1) ends each problem's inner CG once its
  * r'Cr fell by itol^2 (its residual by itol), at most inner_iters. */

@@ -55,7 +55,7 @@ EXPORTS = (
     "nb_time_cg_kernels", "nb_glsc3_noalloc", "nb_time_cg_kernels_f32",
     "nb_batch_create", "nb_batch_destroy", "nb_batch_info", "nb_batch_problem",
     "nb_batch_arrays", "nb_batch_setup", "nb_batch_tune", "nb_batch_get_tuning",
-    "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_set_inner_tol", "nb_batch_result", "nb_batch_cycles",
+    "nb_batch_set_tuning", "nb_batch_solve", "nb_batch_time_phases", "nb_batch_set_inner_tol", "nb_batch_result", "nb_batch_cycles",
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
@@ -116,6 +116,7 @@ for _name, _args in (
         ("nb_batch_get_tuning", [_p, _i, _p, _p, _p, _p, _p]),
         ("nb_batch_set_tuning", [_p, _i, _i, _i, _i]),
         ("nb_batch_solve", [_p, _d, _i, _i]),
+        ("nb_batch_time_phases", [_p, _d, _i, _i, _p, _p]),
         ("nb_batch_set_inner_tol", [_p, _d]),
         ("nb_batch_result", [_p, _i, _p, _p, _p]),
         ("nb_batch_cycles", [_p, _p]),
@@ -613,6 +614,19 @@ class Batch:
     def solve(self, tol: float = 1e-10, inner_iters: int = 20, max_outer: int = 50) -> None:
         """enqueue the whole solve (one graph launch) on the library stream"""
         _check(lib.nb_batch_solve(self._h, _C.c_double(tol), inner_iters, max_outer))
+
+    PHASES = ("init", "scale", "inner_ax", "inner_gs_dot", "inner_update", "defect_ax",
+              "defect_gs_residual")
+
+    def time_phases(self, tol: float = 1e-10, inner_iters: int = 20, max_outer: int = 50):
+        """The solve launched one cycle at a time with an event after every
+        kernel (same kernels, same results; synchronous): ({phase: ms summed
+        over the solve}, cycles)"""
+        ms = (_C.c_double * len(self.PHASES))()
+        cyc = _C.c_int()
+        _check(lib.nb_batch_time_phases(self._h, _C.c_double(tol), inner_iters, max_outer, ms,
+                                        _C.byref(cyc)))
+        return dict(zip(self.PHASES, list(ms))), cyc.value
 
     def result(self, p: int):
         """(cycles, inner iterations, |r|_C/|f|_C) of problem p"""

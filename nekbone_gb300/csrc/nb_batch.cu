@@ -584,22 +584,126 @@ struct Batch {
     return fail(NB_ERR_UNSUPPORTED, "batched solve: lx1=%d not supported", lx);
   }
 
-  // one inner FP32 iteration / the FP64 defect, for all active problems
-  int inner_iteration(int it, int max_inner, cudaStream_t s) const {
+  // Records phase mark e on s (a no-op without one); under stream capture
+  // the record becomes an event node of the graph.
+  static int mark(const cudaEvent_t *e, cudaStream_t s) {
+    if (e) NB_CUDA(cudaEventRecordWithFlags(*e, s, cudaEventRecordExternal));
+    return NB_OK;
+  }
+
+  // one inner FP32 iteration / the FP64 defect, for all active problems;
+  // with mk, an event after each of the iteration's three (the defect's
+  // two) launches
+  int inner_iteration(int it, int max_inner, cudaStream_t s,
+                      const cudaEvent_t *mk = nullptr) const {
     NB_TRY(launch_inner_ax(it, s));
+    NB_TRY(mark(mk, s));
     k_bgs_fin<<<ngc, kThreads, 0, s>>>(w32, p32, c32, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
                                        part_ax, cnt);
     NB_CUDA(cudaGetLastError());
+    NB_TRY(mark(mk ? mk + 1 : nullptr, s));
     k_bupd<<<npc, kThreads, 0, s>>>(e32, r32, p32, w32, c32, pch_q0, pch_prob, pb, sc, part_pt,
                                      cnt + nprob, it, max_inner, itol);
     NB_CUDA(cudaGetLastError());
+    NB_TRY(mark(mk ? mk + 2 : nullptr, s));
     return NB_OK;
   }
-  int defect(double tol, int max_outer, cudaStream_t s) const {
+  int defect(double tol, int max_outer, cudaStream_t s, const cudaEvent_t *mk = nullptr) const {
     NB_TRY(launch_defect_ax(s));
+    NB_TRY(mark(mk, s));
     k_bgs_res<<<ngc, kThreads, 0, s>>>(w, x, f, r, c, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
                                        part_ax, cnt + 2 * nprob, tol, max_outer);
     NB_CUDA(cudaGetLastError());
+    NB_TRY(mark(mk ? mk + 1 : nullptr, s));
+    return NB_OK;
+  }
+  int scale(cudaStream_t s) const {
+    k_bscale<<<npc, kThreads, 0, s>>>(r32, e32, r, c32, pch_q0, pch_prob, pb, sc, part_pt,
+                                      cnt + 3 * nprob);
+    NB_CUDA(cudaGetLastError());
+    return NB_OK;
+  }
+  int init(int max_outer, cudaStream_t s) const {
+    k_binit<<<npc, kThreads, 0, s>>>(x, r, f, c, pch_q0, pch_prob, pb, sc, part_pt,
+                                     cnt + 3 * nprob, max_outer);
+    NB_CUDA(cudaGetLastError());
+    return NB_OK;
+  }
+
+  // The solve of build_graph launched one cycle at a time: each cycle is a
+  // graph of the same kernels with an event after every launch, and the
+  // loop condition (some problem active, fewer than max_outer + 1 cycles)
+  // is read on the host between cycles.  Adds each phase's device time
+  // (kBatchPhases entries, nb_batch_time_phases's order) to ms.
+  static constexpr int kBatchPhases = 7;
+  int timed_solve(double tol, int inner, int max_outer, cudaStream_t s, double *ms,
+                  int *ncyc) {
+    struct Owned {
+      std::vector<cudaEvent_t> ev;
+      cudaGraph_t g = nullptr;
+      cudaGraphExec_t x = nullptr;
+      ~Owned() {
+        if (x) cudaGraphExecDestroy(x);
+        if (g) cudaGraphDestroy(g);
+        for (cudaEvent_t e : ev) cudaEventDestroy(e);
+      }
+    } o;
+    // events: start, after scale, 3 per inner iteration, 2 for the defect
+    const int nev = 3 * inner + 4;
+    std::vector<int> phase(nev, -1);   // phase of the interval ending at event q
+    phase[1] = 1;
+    for (int it = 0; it < inner; ++it)
+      for (int k = 0; k < 3; ++k) phase[2 + 3 * it + k] = 2 + k;
+    phase[nev - 2] = 5;
+    phase[nev - 1] = 6;
+    for (int q = 0; q < nev; ++q) {
+      cudaEvent_t e;
+      NB_CUDA(cudaEventCreate(&e));
+      o.ev.push_back(e);
+    }
+    if (!cap) NB_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    NB_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed));
+    int st = mark(&o.ev[0], cap);
+    if (!st) st = scale(cap);
+    if (!st) st = mark(&o.ev[1], cap);
+    for (int it = 1; it <= inner && !st; ++it)
+      st = inner_iteration(it, inner, cap, &o.ev[2 + 3 * (it - 1)]);
+    if (!st) st = defect(tol, max_outer, cap, &o.ev[nev - 2]);
+    const cudaError_t ce = cudaStreamEndCapture(cap, &o.g);
+    if (st) return st;
+    if (ce != cudaSuccess)
+      return fail(NB_ERR_CUDA, "batched phase timing: capture: %s", cudaGetErrorString(ce));
+    NB_CUDA(cudaGraphInstantiate(&o.x, o.g, 0));
+    cudaEvent_t i0 = o.ev[0], i1 = o.ev[1];
+    NB_CUDA(cudaEventRecord(i0, s));
+    NB_TRY(init(max_outer, s));
+    NB_CUDA(cudaEventRecord(i1, s));
+    NB_CUDA(cudaEventSynchronize(i1));
+    float t = 0.f;
+    NB_CUDA(cudaEventElapsedTime(&t, i0, i1));
+    ms[0] += t;
+    std::vector<BatchScalars> h(nprob);
+    const int max_cycles = max_outer + 1;
+    int cyc = 0;
+    for (;;) {
+      NB_CUDA(cudaMemcpyAsync(h.data(), sc, nprob * sizeof(BatchScalars),
+                              cudaMemcpyDeviceToHost, s));
+      NB_CUDA(cudaStreamSynchronize(s));
+      int any = 0;
+      for (const BatchScalars &q : h) any |= q.active;
+      if (!any || cyc >= max_cycles) break;
+      NB_CUDA(cudaGraphLaunch(o.x, s));
+      NB_CUDA(cudaEventSynchronize(o.ev[nev - 1]));
+      for (int q = 1; q < nev; ++q) {
+        NB_CUDA(cudaEventElapsedTime(&t, o.ev[q - 1], o.ev[q]));
+        ms[phase[q]] += t;
+      }
+      ++cyc;
+    }
+    NB_CUDA(cudaMemcpyAsync(cycles, &cyc, sizeof(int), cudaMemcpyHostToDevice, s));
+    NB_CUDA(cudaStreamSynchronize(s));
+    NB_TRY(device_error_check(s));
+    *ncyc = cyc;
     return NB_OK;
   }
 
@@ -623,12 +727,12 @@ struct Batch {
     // the graph that owns the handle)
     NB_CUDA(cudaStreamBeginCaptureToGraph(cap, G, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    k_binit<<<npc, kThreads, 0, cap>>>(x, r, f, c, pch_q0, pch_prob, pb, sc, part_pt,
-                                       cnt + 3 * nprob, max_outer);
-    k_bcontrol<<<1, kThreads, 0, cap>>>(sc, nprob, cycles, 1, max_cycles, h);
     {
+      const int st0 = init(max_outer, cap);
+      k_bcontrol<<<1, kThreads, 0, cap>>>(sc, nprob, cycles, 1, max_cycles, h);
       cudaGraph_t got = nullptr;
       NB_CUDA(cudaStreamEndCapture(cap, &got));
+      NB_TRY(st0);
     }
     // the loop follows the capture's last node (the one without dependents)
     size_t nn = 0;
@@ -652,10 +756,7 @@ struct Batch {
     // one cycle: scale, inner CG, FP64 defect, loop condition
     NB_CUDA(cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeRelaxed));
-    int st = NB_OK;
-    k_bscale<<<npc, kThreads, 0, cap>>>(r32, e32, r, c32, pch_q0, pch_prob, pb, sc, part_pt,
-                                        cnt + 3 * nprob);
-    if (cudaGetLastError() != cudaSuccess) st = fail(NB_ERR_CUDA, "batched solve: capture");
+    int st = scale(cap);
     for (int it = 1; it <= inner && !st; ++it) st = inner_iteration(it, inner, cap);
     if (!st) st = defect(tol, max_outer, cap);
     if (!st) {
@@ -1132,6 +1233,22 @@ int nb_batch_solve(nb_batch *b, double tol, int inner_iters, int max_outer) {
                 max_outer);
   NB_TRY(B.build_graph(tol, inner_iters, max_outer));
   NB_CUDA(cudaGraphLaunch(B.exec, lib_stream()));
+  return NB_OK;
+}
+
+int nb_batch_time_phases(nb_batch *b, double tol, int inner_iters, int max_outer, double *ms,
+                         int *cycles) {
+  clear_status();
+  if (!b || !ms) return fail(NB_ERR_ARG, "nb_batch_time_phases: null argument");
+  Batch &B = b->B;
+  if (!B.setup_done) return fail(NB_ERR_STATE, "nb_batch_time_phases: call nb_batch_setup first");
+  if (inner_iters < 1 || max_outer < 0 || !(tol >= 0.0))
+    return fail(NB_ERR_ARG, "nb_batch_time_phases: inner_iters=%d max_outer=%d", inner_iters,
+                max_outer);
+  for (int k = 0; k < Batch::kBatchPhases; ++k) ms[k] = 0.0;
+  int cyc = 0;
+  NB_TRY(B.timed_solve(tol, inner_iters, max_outer, lib_stream(), ms, &cyc));
+  if (cycles) *cycles = cyc;
   return NB_OK;
 }
 

@@ -247,3 +247,30 @@ def test_inner_tolerance_stops_each_problem(torch):
         outer, inner, rr = b.result(p)
         assert inner == 20 * outer and rr <= 1e-10
     b.close()
+
+
+def test_phase_timing_runs_the_same_solve(torch):
+    """nb_batch_time_phases launches the graph solve's kernels one cycle at a
+    time with events between them: bit-identical x and per-problem results,
+    the same cycle count, and a positive time for every phase that ran."""
+    import nekbone_gb300 as nb
+    b = nb.Batch(BOXES)
+    b.setup(17)
+    b.tune(1)
+    b.set_inner_tol(1e-4)
+    b.solve(1e-10, 30, 40)
+    nb.sync()
+    x_graph = _view(torch, b.arrays()[0], b.n).cpu().numpy().copy()
+    res_graph = [b.result(p) for p in range(b.nprob)]
+    cyc_graph = b.cycles()
+    _view(torch, b.arrays()[0], b.n).fill_(float("nan"))
+    torch.cuda.synchronize()
+    ms, cyc = b.time_phases(1e-10, 30, 40)
+    x = _view(torch, b.arrays()[0], b.n).cpu().numpy()
+    assert cyc == cyc_graph == b.cycles() and cyc >= 2
+    assert np.array_equal(x, x_graph)
+    assert [b.result(p) for p in range(b.nprob)] == res_graph
+    assert set(ms) == set(nb.Batch.PHASES)
+    assert all(v > 0.0 for v in ms.values()), ms
+    print("batched phases (ms):", {k: round(v, 4) for k, v in ms.items()})
+    b.close()

@@ -174,3 +174,64 @@ def test_hsmg_solve_and_pcg():
     out = ctx2.cg(f, ctx2.setup_g(), c, niter, use_mg=True)
     assert _rel(out["x"], g["pcg_x"]) < 1e-10
     _check_history(out["hist"], g["pcg_log"], exact=False)
+
+
+def _trace_meshes(z):
+    """Per mesh of a driver trace: the nekbone_common values and the
+    indices of the calls that follow it up to the next mesh."""
+    import json
+    calls = json.loads(str(z["calls"]))
+    meshes = []
+    for k, call in enumerate(calls):
+        if call["name"] == "nekbone_mask_reset":      # init_mesh starts a mesh
+            meshes.append(dict(calls=[]))
+        if call["name"] == "nekbone_common":
+            meshes[-1].update(dims=[int(z[f"c{k}_a{j}_in"][0]) for j in range(5)],
+                              lglel=z[f"c{k}_a5_in"], dxm1=z[f"c{k}_a6_in"])
+        meshes[-1]["calls"].append((k, call["name"]))
+    return calls, meshes
+
+
+@pytest.mark.parametrize("tag", ["plain", "mgrid"])
+def test_driver_program_trace_matches_oracle(tag):
+    """The boundary calls of driver.f's own program (make_golden_driver.py)
+    against the oracle: per mesh, the published dxm1 and the cg inputs (c, f,
+    g) are the oracle's set-up, set_multiplicity's gs_op returns the counts,
+    and the warm-up and timed cg return the oracle's x and r -- bit for bit
+    without the preconditioner, to 1e-12 with hsmg (two eigensolvers)."""
+    z = _load(f"driver_trace_{tag}.npz")
+    calls, meshes = _trace_meshes(z)
+    names = [c["name"] for c in calls]
+    # driver.f's order per mesh: init_mesh's reset, proxy_setupds's
+    # gs_setup, set_multiplicity's gs_op, the hand-off after proxy_setup,
+    # h1mg_setup, set_f's dssum, the two cg calls, gs_free
+    per_mesh = ["nekbone_mask_reset", "gs_setup", "gs_op", "nekbone_common",
+                "nekbone_set_mask_mode", "nekbone_set_mgrid", "h1mg_setup", "dssum", "cg", "cg",
+                "gs_free"]
+    assert names == per_mesh * len(meshes)
+    mg = tag == "mgrid"
+    for m in meshes:
+        nelx, nely, nelz, nelt, nx1 = m["dims"]
+        assert nelx * nely * nelz == nelt
+        ctx = O.Ctx(nelx, nely, nelz, nx1, mask_mode=0, lglel=m["lglel"], fma=False)
+        assert np.array_equal(ctx.dxm1(), m["dxm1"])
+        if mg:
+            assert ctx.h1mg_setup() == 0
+        c = ctx.set_multiplicity()
+        f = ctx.set_f(c)
+        g = ctx.setup_g()
+        cg_calls = [k for k, name in m["calls"] if name == "cg"]
+        k_op = [k for k, name in m["calls"] if name == "gs_op"][0]
+        assert np.array_equal(1.0 / z[f"c{k_op}_a1_out"], c)
+        work = tuple(np.zeros(ctx.n) for _ in range(5))
+        for k in cg_calls:
+            assert int(z[f"c{k}_a8_in"][0]) == ctx.n and int(z[f"c{k}_a9_in"][0]) == 100
+            assert np.array_equal(z[f"c{k}_a3_in"], c)
+            assert np.array_equal(z[f"c{k}_a1_in"], f)
+            assert np.array_equal(z[f"c{k}_a2_in"], g)
+            out = ctx.cg(f, g, c, 100, use_mg=mg, work=work)
+            if mg:
+                assert _rel(out["x"], z[f"c{k}_a0_out"]) < 1e-12
+            else:
+                assert np.array_equal(out["x"], z[f"c{k}_a0_out"]), k
+                assert np.array_equal(out["r"], z[f"c{k}_a4_out"]), k
