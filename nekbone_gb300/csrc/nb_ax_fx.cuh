@@ -45,13 +45,14 @@
 
 #include "nb_kernels.cuh"
 
-// CTAs per SM of the fixed-point operator at lx1 <= 12 (its four
-// shared-memory arrays, 56 KB at lx1 = 12, allow four: 2.01 ms at 32^3
-// against 2.25 ms with rows padded to lx1 + 1 and three CTAs); the output
-// rows of a line are unrolled two at a time (fully unrolled, the kernel
-// spills and measures slower)
+// CTAs per SM of the fixed-point operator at lx1 <= 12: its three
+// shared-memory arrays (42 KB at lx1 = 12) allow five, and the bound keeps
+// the registers within five (1.90 ms at 32^3, against 2.01 ms with four
+// arrays and four CTAs, 2.25 ms with rows padded to lx1 + 1 and three).
+// The output rows of a line are unrolled two at a time (fully unrolled,
+// the kernel spills and measures slower).
 #ifndef NB_FX_MINB
-#define NB_FX_MINB 4
+#define NB_FX_MINB 5
 #endif
 #ifndef NB_FX_AUNROLL
 #define NB_FX_AUNROLL 2
@@ -174,7 +175,6 @@ template <int LX>
 struct FxShared {
   static constexpr int N = (LX * LX + 1) * LX;
   i64 A[N];
-  i64 B[N];
   i64 C[N];
   i64 D[N];
   int emax[8];
@@ -305,13 +305,16 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   // code per stage; every output goes to shared memory.
   const int lb0 = fx_at<LX>(0, j, i), lb1 = fx_at<LX>(i, 0, j), lb2 = fx_at<LX>(i, j, 0);
 
-  // gradient (local_grad3): A -> B (ur), C (us), D (ut)
+  // gradient (local_grad3): A -> C (us), D (ut); then, once every s- and
+  // t-line of A was read, A -> A (ur) line by line in place
   u64 orv = 0;
 #pragma unroll 1
-  for (int d = 0; d < 3; ++d) {
+  for (int dd = 0; dd < 3; ++dd) {
+    const int d = dd == 2 ? 0 : dd + 1;
+    if (dd == 2) __syncthreads();
     const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
     const int st = d == 0 ? 1 : d == 1 ? LX : (LX * LX + 1);
-    i64 *out = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
+    i64 *out = d == 0 ? sm.A : d == 1 ? sm.C : sm.D;
     i64 v[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = sm.A[b0 + m * st];
@@ -329,10 +332,10 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int eg = a.gexp[e];
   const int sW = 64 + (eg - 1082) + sU;  // wr = WR 2^sW before renormalising
   orv = 0;
-#pragma unroll 2
+#pragma unroll 4
   for (int k = 0; k < LX; ++k) {
     const int q = fx_at<LX>(i, j, k);
-    const Sp ur = split(shift_signed(sm.B[q], s1)), us = split(shift_signed(sm.C[q], s1)),
+    const Sp ur = split(shift_signed(sm.A[q], s1)), us = split(shift_signed(sm.C[q], s1)),
              ut = split(shift_signed(sm.D[q], s1));
     const int4 *gp = reinterpret_cast<const int4 *>(a.gfx + 6 * (base + size_t(k) * L2 + t));
     const int4 g01 = __ldg(gp), g23 = __ldg(gp + 1), g45 = __ldg(gp + 2);
@@ -343,7 +346,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
     ws.mac(G2, ur); ws.mac(G4, us); ws.mac(G5, ut);
     wt.mac(G3, ur); wt.mac(G5, us); wt.mac(G6, ut);
     const i64 r_ = wr.result(), s_ = ws.result(), t_ = wt.result();
-    sm.B[q] = r_;
+    sm.A[q] = r_;
     sm.C[q] = s_;
     sm.D[q] = t_;
     orv |= mag(r_) | mag(s_) | mag(t_);
@@ -353,19 +356,17 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int s2 = fx_or_shift(sm.orl, sm.orh, L2);
   const int sT = 64 - fc + sW - s2;  // transposed-gradient outputs: value 2^sT
 
-  // transposed gradient (local_grad3_t) with D^T: B -> A (tr); after every
-  // r-line of B was read, C -> B (ts); D -> D (tt: the own column, read and
-  // written by this thread alone)
+  // transposed gradient (local_grad3_t) with D^T, each line in place: A
+  // (tr), C (ts), D (tt); a thread reads and writes only its own lines
 #pragma unroll 1
   for (int d = 0; d < 3; ++d) {
     const int b0 = d == 0 ? lb0 : d == 1 ? lb1 : lb2;
     const int st = d == 0 ? 1 : d == 1 ? LX : (LX * LX + 1);
-    const i64 *src = d == 0 ? sm.B : d == 1 ? sm.C : sm.D;
-    i64 *out = d == 0 ? sm.A : d == 1 ? sm.B : sm.D;
+    i64 *out = d == 0 ? sm.A : d == 1 ? sm.C : sm.D;
+    const i64 *src = out;
     i64 v[LX];
 #pragma unroll
     for (int m = 0; m < LX; ++m) v[m] = shift_signed(src[b0 + m * st], s2);
-    if (d == 1) __syncthreads();
     fx_line<LX>(v, cf, 2 * H * H, [&](int m, i64 y) { out[b0 + m * st] = y; });
   }
   __syncthreads();
@@ -388,7 +389,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
     const int q = fx_at<LX>(i, j, k);
-    double wl = to_double(sm.A[q] + sm.B[q] + sm.D[q], sT);
+    double wl = to_double(sm.A[q] + sm.C[q] + sm.D[q], sT);
     const size_t id = base + size_t(k) * L2 + t;
     const bool interior = col_interior && (k > 0) && (k < LX - 1);
     if (MODE == 1) {
@@ -415,8 +416,10 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   }
 }
 
+// (the thread bound is the whole warps the block occupies, so that the
+// register budget per thread is what NB_FX_MINB resident blocks leave)
 template <int LX, int MODE>
-__global__ void __launch_bounds__(LX * LX, (LX <= 12 ? NB_FX_MINB : 1))
+__global__ void __launch_bounds__((LX * LX + 31) / 32 * 32, (LX <= 12 ? NB_FX_MINB : 1))
     k_ax_fx(AxArgs<double> a, const __grid_constant__ FxCoef<LX> cf) {
   ax_fx_body<LX, MODE>(a, cf);
 }
