@@ -375,7 +375,9 @@ int nb_batch_setup(nb_batch *batch, uint64_t seed);
 /* Autotuner: times every instantiated shape (elements per block, D in
  * registers or shared memory) of the FP32 inner and FP64 defect element
  * operators on the batch's elements of each lx1, reps launches each, and
- * keeps the fastest.  Overwrites x. */
+ * keeps the fastest.  Overwrites x.  The FP64 defect's shapes: epb64 = -1
+ * the fixed-point form on the integer pipes (the default before tuning),
+ * 0 the even-odd form on the FP64 pipe, > 0 elements per block. */
 int nb_batch_tune(nb_batch *batch, int reps);
 int nb_batch_get_tuning(const nb_batch *batch, int lx1, int *epb32, int *rd32, int *epb64,
                         float *ms32, float *ms64);

@@ -253,6 +253,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
   const int e = blockIdx.x;
   const size_t base = size_t(e) * L3;
   const int fc = cf.fc;
+  if (a.act && !a.act[size_t(a.el_prob[e]) * a.act_stride]) return;  // the whole CTA
 
   // direction update (MODE 1) / correction (MODE 2), in FP64, then the
   // element's exponent and its fixed-point block

@@ -267,6 +267,22 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// x += |r| e for every active problem: the correction step of the FP64
+// defect when the element operator is the fixed-point form (which takes x
+// already corrected); the same fused multiply-add as the FP64-pipe forms'
+// prologue.
+__global__ void __launch_bounds__(kThreads)
+    k_bxupd(double *__restrict__ x, const float *__restrict__ e, const long *__restrict__ pch_q0,
+            const int *__restrict__ pch_prob, const BatchScalars *__restrict__ sc) {
+  const int ch = blockIdx.x;
+  const int prob = pch_prob[ch];
+  if (!sc[prob].active) return;
+  const double scale = sc[prob].rn;
+  const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
+  for (long q = q0 + threadIdx.x; q < q1; q += kThreads)
+    x[q] = fma_rn(scale, double(e[q]), x[q]);
+}
+
 // Initial state: x = 0, r = f, |f|_C; a problem with f = 0 (or no cycles
 // allowed) is inactive from the start.
 __global__ void __launch_bounds__(kThreads)
@@ -468,9 +484,13 @@ struct Batch {
   struct Group {
     int lx = 0, el0 = 0, nel = 0;
     long pt0 = 0, n = 0;
+    int pc0 = 0, npc = 0;     // its point chunks
     double *D64 = nullptr;
     float *D32 = nullptr;
     std::vector<double> EO;   // even-odd tables (host; empty for odd lx1)
+    // the fixed-point FP64 operator's tables and converted metric for this
+    // group's elements (even lx1)
+    std::shared_ptr<Operator> fx;
     BatchTune tune;
   };
   int nprob = 0;
@@ -539,28 +559,60 @@ struct Batch {
     }
     return NB_OK;
   }
-  int launch_defect_ax(cudaStream_t s) const {
-    for (const auto &G : groups) {
-      BaxArgs<double> a{};
-      a.w = w;
-      a.p = x;
-      a.g = g;
-      a.c = c;
-      a.D = G.D64;
-      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
-      a.f = f;
-      a.r = r;
-      a.e = e32;
-      a.el_prob = el_prob;
-      a.sc = sc;
-      a.partial = part_ax;
-      a.pt0 = G.pt0;
-      a.el0 = G.el0;
-      a.nel = G.nel;
-      a.err = device_error_word();
-      a.wait_test = wait_test_mode();
-      NB_TRY(batch_ax_f64(G.lx, G.tune.epb64, a, s));
+  // The FP64 defect's element operator for one group in shape epb64
+  // (kFxShape: the fixed-point form after a separate x += |r| e).
+  int defect_group_ax(const Group &G, int epb64, cudaStream_t s) const {
+    if (epb64 == kFxShape) {
+      if (!G.fx) return fail(NB_ERR_UNSUPPORTED, "batched solve: no fixed-point form for lx1=%d",
+                             G.lx);
+      k_bxupd<<<G.npc, kThreads, 0, s>>>(x, e32, pch_q0 + G.pc0, pch_prob + G.pc0, sc);
+      NB_CUDA(cudaGetLastError());
+      AxArgs<double> a{};
+      a.w = w + G.pt0;
+      a.p = x + G.pt0;
+      a.c = c + G.pt0;
+      a.f = f + G.pt0;
+      a.r = r + G.pt0;
+      a.partial = part_ax + G.el0;
+      a.nelt = G.nel;
+      a.gfx = G.fx->gfx;
+      a.gexp = G.fx->gexp;
+      a.el_prob = el_prob + G.el0;
+      a.act = &sc[0].active;
+      a.act_stride = int(sizeof(BatchScalars) / sizeof(int));
+      return launch_ax_fx_m2(*G.fx, a, s);
     }
+    BaxArgs<double> a{};
+    a.w = w;
+    a.p = x;
+    a.g = g;
+    a.c = c;
+    a.D = G.D64;
+    a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
+    a.f = f;
+    a.r = r;
+    a.e = e32;
+    a.el_prob = el_prob;
+    a.sc = sc;
+    a.partial = part_ax;
+    a.pt0 = G.pt0;
+    a.el0 = G.el0;
+    a.nel = G.nel;
+    a.err = device_error_word();
+    a.wait_test = wait_test_mode();
+    return batch_ax_f64(G.lx, epb64, a, s);
+  }
+  // the fixed-point metric of every group that uses the fixed-point form
+  int convert_metric(cudaStream_t s) const {
+    for (const auto &G : groups)
+      if (G.fx && G.tune.epb64 == kFxShape) {
+        metric_fx_invalidate(*G.fx);
+        NB_TRY(metric_fx_prepare(*G.fx, g + 6 * G.pt0, s));
+      }
+    return NB_OK;
+  }
+  int launch_defect_ax(cudaStream_t s) const {
+    for (const auto &G : groups) NB_TRY(defect_group_ax(G, G.tune.epb64, s));
     return NB_OK;
   }
   static int batch_ax_f32(int lx, int epb, int rd, const BaxArgs<float> &a, cudaStream_t s) {
@@ -623,7 +675,10 @@ struct Batch {
     NB_CUDA(cudaGetLastError());
     return NB_OK;
   }
+  // initial norms, and the fixed-point metric of the solve (g may have
+  // changed since the last one)
   int init(int max_outer, cudaStream_t s) const {
+    NB_TRY(convert_metric(s));
     k_binit<<<npc, kThreads, 0, s>>>(x, r, f, c, pch_q0, pch_prob, pb, sc, part_pt,
                                      cnt + 3 * nprob, max_outer);
     NB_CUDA(cudaGetLastError());
@@ -740,12 +795,16 @@ struct Batch {
     std::vector<cudaGraphNode_t> nodes(nn);
     NB_CUDA(cudaGraphGetNodes(G, nodes.data(), &nn));
     cudaGraphNode_t ninit = nullptr;
+    int nlast = 0;
     for (cudaGraphNode_t q : nodes) {
       size_t nd = 0;
       NB_CUDA(cudaGraphNodeGetDependentNodes(q, nullptr, nullptr, &nd));
-      if (nd == 0) ninit = q;
+      if (nd == 0) {
+        ninit = q;
+        ++nlast;
+      }
     }
-    if (nn != 2 || !ninit) return fail(NB_ERR_CUDA, "batched solve: unexpected initial graph");
+    if (nlast != 1) return fail(NB_ERR_CUDA, "batched solve: unexpected initial graph");
     cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
     cp.conditional.handle = h;
     cp.conditional.type = cudaGraphCondTypeWhile;
@@ -879,10 +938,12 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
       G.lx = lx[p];
       G.el0 = Q.el0;
       G.pt0 = Q.pt0;
+      G.pc0 = Q.pc0;
       B->groups.push_back(G);
     }
     B->groups.back().nel += int(nelt);
     B->groups.back().n += Q.n;
+    B->groups.back().npc += Q.npc;
   }
   off_all.push_back(int(idx_all.size()));
   gch_g0.push_back(gbase);
@@ -929,6 +990,12 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
     NB_TRY(upload(&G.D64, d));
     NB_TRY(upload(&G.D32, d32));
     if (!even_odd_tables(d, L, G.EO)) G.EO.clear();
+    auto op = std::make_shared<Operator>();
+    op->lx = L;
+    op->n = G.n;
+    op->nelt = G.nel;
+    op->fx_ok = fx_tables(d, L, op->FXhi, op->FXlo, &op->fx_fc);
+    if (op->fx_ok) G.fx = op;
     // default shape: the first listed (the even-odd form where lx1 is even)
     const auto s32 = batch_shapes_f32(L);
     const auto s64 = batch_shapes_f64(L);
@@ -959,7 +1026,8 @@ std::vector<std::pair<int, int>> batch_shapes_f32(int lx) {
 
 std::vector<int> batch_shapes_f64(int lx) {
   std::vector<int> out;
-  if (lx % 2 == 0) out.push_back(0);   // even-odd form
+  if (lx % 2 == 0) out.push_back(kFxShape);   // fixed point on the integer pipes
+  if (lx % 2 == 0) out.push_back(0);          // even-odd form on the FP64 pipe
   switch (lx) {
     case 4: out.insert(out.end(), {4, 8}); break;
     case 6: out.insert(out.end(), {2, 4}); break;
@@ -1061,6 +1129,13 @@ int nb_batch_setup(nb_batch *b, uint64_t seed) {
   k_conv<float, double><<<grid_for(6 * B.n), 256, 0, s>>>(B.g32, B.g, 6 * B.n);
   k_conv<float, double><<<grid_for(B.n), 256, 0, s>>>(B.c32, B.c, B.n);
   NB_CUDA(cudaGetLastError());
+  // the fixed-point metric (allocated here, outside any graph capture;
+  // every solve converts it again)
+  for (auto &G : B.groups)
+    if (G.fx) {
+      metric_fx_invalidate(*G.fx);
+      NB_TRY(metric_fx_prepare(*G.fx, B.g + 6 * G.pt0, s));
+    }
   NB_CUDA(cudaStreamSynchronize(s));
   B.setup_done = true;
   return NB_OK;
@@ -1166,28 +1241,10 @@ int nb_batch_tune(nb_batch *b, int reps) {
     if (st) break;
     best = 1e30f;
     for (int epb : batch_shapes_f64(G.lx)) {
-      BaxArgs<double> a{};
-      a.w = B.w;
-      a.p = B.x;
-      a.g = B.g;
-      a.c = B.c;
-      a.D = G.D64;
-      a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
-      a.f = B.f;
-      a.r = B.r;
-      a.e = B.e32;
-      a.el_prob = B.el_prob;
-      a.sc = B.sc;
-      a.partial = B.part_ax;
-      a.pt0 = G.pt0;
-      a.el0 = G.el0;
-      a.nel = G.nel;
-      a.err = device_error_word();
-      a.wait_test = wait_test_mode();
-      st = Batch::batch_ax_f64(G.lx, epb, a, s);
+      st = B.defect_group_ax(G, epb, s);
       if (st) break;
       cudaEventRecord(e0, s);
-      for (int q = 0; q < reps; ++q) Batch::batch_ax_f64(G.lx, epb, a, s);
+      for (int q = 0; q < reps; ++q) B.defect_group_ax(G, epb, s);
       cudaEventRecord(e1, s);
       cudaEventSynchronize(e1);
       float ms = 0.f;

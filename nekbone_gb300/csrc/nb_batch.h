@@ -77,8 +77,13 @@ template <int LX>
 int batch_ax_f32_lx(int epb, int rd, const BaxArgs<float> &a, cudaStream_t s);
 template <int LX>
 int batch_ax_f64_lx(int epb, const BaxArgs<double> &a, cudaStream_t s);
+// The FP64 defect operator's shape value for the fixed-point form (even
+// lx1): x += |r| e by a streaming kernel, then the fixed-point element
+// operator (nb_ax_fx.cuh) on the group's elements.
+constexpr int kFxShape = -1;
 // instantiated shapes for lx1 = lx: (elements per block, register D) for the
-// FP32 operator, elements per block for the FP64 one
+// FP32 operator, elements per block for the FP64 one (0: the even-odd form,
+// kFxShape: fixed point)
 std::vector<std::pair<int, int>> batch_shapes_f32(int lx);
 std::vector<int> batch_shapes_f64(int lx);
 

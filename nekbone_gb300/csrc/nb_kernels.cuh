@@ -123,6 +123,9 @@ struct AxArgs {
   int wait_test;     // timeout self-test of the bulk-copy wait (block_copy_begin)
   const int2 *gfx;   // fixed-point FP64 operator: the metric in fixed point
   const int *gexp;   //   and each element's exponent (metric_fx_prepare)
+  const int *el_prob;  // fixed-point operator in a batched solve: element e is
+  const int *act;      //   skipped when act[el_prob[e] * act_stride] is 0 (its
+  int act_stride;      //   problem is no longer active); null for one mesh
 };
 
 template <typename T, int LX>

@@ -148,6 +148,9 @@ template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s);
 template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s);
+// The fixed-point FP64 operator in MODE 2 on op's tables (op.lx, FXhi,
+// FXlo, fx_fc) for a.nelt elements; a.gfx / a.gexp set by the caller.
+int launch_ax_fx_m2(const Operator &op, AxArgs<double> a, cudaStream_t s);
 template <typename T>
 int vec_glsc3(const T *a, const T *b, const T *m, long n, CgWork &wk,
               double *out, CgScalars *sc, int mode, int iter, cudaStream_t s,

@@ -274,3 +274,31 @@ def test_phase_timing_runs_the_same_solve(torch):
     assert all(v > 0.0 for v in ms.values()), ms
     print("batched phases (ms):", {k: round(v, 4) for k, v in ms.items()})
     b.close()
+
+
+def test_fixed_point_defect_operator(torch):
+    """The FP64 defect in the fixed-point form (epb64 = -1: x += |r| e, then
+    the fixed-point element operator on the integer pipes) against the
+    even-odd FP64-pipe form: both meet the tolerance by the oracle's own
+    residual, and the solutions agree to 1e-8 (the two operators agree to
+    rounding, ~1e-15 per apply)."""
+    import nekbone_gb300 as nb
+    b = nb.Batch(BOXES)
+    b.setup(17)
+    xs = []
+    for epb64 in (-1, 0):
+        for lx in sorted({bx[3] for bx in BOXES}):
+            t = b.tuning(lx)
+            b.set_tuning(lx, t["epb32"], t["rd32"], epb64)
+            assert b.tuning(lx)["epb64"] == epb64
+        b.solve(1e-10, 20, 40)
+        nb.sync()
+        xs.append(_view(torch, b.arrays()[0], b.n).cpu().numpy().copy())
+        for p, (nx, ny, nz, lx) in enumerate(BOXES):
+            a = _problem_arrays(torch, b, p)
+            ctx = O.Ctx(nx, ny, nz, lx, mask_mode=1)
+            r = a["f"] - ctx.ax(a["x"], a["g"])
+            rel = np.sqrt(np.sum(r * a["c"] * r)) / np.sqrt(np.sum(a["f"] * a["c"] * a["f"]))
+            assert rel <= 2e-10, (epb64, p, rel)
+    assert np.max(np.abs(xs[0] - xs[1])) <= 1e-8 * np.max(np.abs(xs[1]))
+    b.close()

@@ -1,0 +1,102 @@
+"""The headline workload at its full size (32^3 elements, lx1 = 12, n =
+56,623,104), checked through properties that do not need the oracle to run
+at that size (the oracle's own check of the first iterations at this size
+runs in bench.py's cpu_check):
+
+* the fixed-point FP64 operator (order 2, the default) and the even-odd FP64
+  operator (order 1) agree per apply to 2e-14 of max|w| (both are the
+  reference's sums to rounding; their difference at 16^3 is ~5e-15);
+* the assembled, masked operator is symmetric in the multiplicity-weighted
+  inner product on continuous masked vectors, v'C(Au) = u'C(Av), to 1e-12
+  relative, and positive;
+* it is linear: A(u + v/2) = Au + Av/2 to 1e-14 of max|Au|;
+* 100 CG iterations in the two operator forms give solutions within 1e-10
+  relative and residual histories within 1e-8 relative, each decreasing by
+  at least 1e3.
+"""
+from __future__ import annotations
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NEL, LX = 32, 12
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def case(torch):
+    import nekbone_gb300 as nb
+    m = nb.DeviceMesh(NEL, NEL, NEL, LX, mask_mode=1)
+    n = m.n
+    assert n == 56623104
+    dev = torch.device("cuda", 0)
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g(g.data_ptr())
+    m.set_multiplicity(c.data_ptr())
+    u = torch.empty(n, dtype=torch.float64, device=dev)
+    v = torch.empty(n, dtype=torch.float64, device=dev)
+    m.rhs_uniform(u.data_ptr(), c.data_ptr(), 11)   # continuous, masked
+    m.rhs_uniform(v.data_ptr(), c.data_ptr(), 12)
+    torch.cuda.synchronize()
+    yield nb, m, g, c, u, v
+    m.set_order(nb.DEFAULT_ORDER)
+    m.close()
+    torch.cuda.empty_cache()
+
+
+def _apply(torch, m, g, u, order):
+    m.set_order(order)
+    w = torch.empty_like(u)
+    m.ax(w.data_ptr(), u.data_ptr(), g.data_ptr())
+    torch.cuda.synchronize()
+    return w
+
+
+def test_fullsize_operator_forms_agree(torch, case):
+    nb, m, g, c, u, v = case
+    w2 = _apply(torch, m, g, u, 2)
+    w1 = _apply(torch, m, g, u, 1)
+    err = float((w2 - w1).abs().max() / w1.abs().max())
+    print(f"32^3 lx1=12: fixed point vs FP64 even-odd apply {err:.2e}")
+    assert err <= 2e-14
+
+
+def test_fullsize_operator_symmetric_positive_linear(torch, case):
+    nb, m, g, c, u, v = case
+    au = _apply(torch, m, g, u, 2)
+    av = _apply(torch, m, g, v, 2)
+    a = float((v * c * au).sum())
+    b = float((u * c * av).sum())
+    print(f"v'C(Au) = {a:.16e}, u'C(Av) = {b:.16e}")
+    assert abs(a - b) <= 1e-12 * abs(a)
+    assert float((u * c * au).sum()) > 0 and float((v * c * av).sum()) > 0
+    s = u + 0.5 * v
+    asum = _apply(torch, m, g, s, 2)
+    err = float((asum - (au + 0.5 * av)).abs().max() / au.abs().max())
+    assert err <= 1e-14
+
+
+def test_fullsize_cg_operator_forms_agree(torch, case):
+    nb, m, g, c, u, v = case
+    f = u
+    xs, hs = [], []
+    for order in (2, 1):
+        m.set_order(order)
+        x, r, w, p, z = (torch.zeros_like(f) for _ in range(5))
+        h = m.cg(*(t.data_ptr() for t in (x, f, g, c, r, w, p, z)), 100, hist=True)
+        torch.cuda.synchronize()
+        xs.append(x)
+        hs.append(h[:, 0])
+        assert h[-1, 0] <= 1e-3 * h[0, 0]
+        del r, w, p, z
+    err = float((xs[0] - xs[1]).abs().max() / xs[1].abs().max())
+    herr = float(abs(hs[0] - hs[1]).max() / hs[1][0])
+    print(f"32^3 lx1=12, 100 CG iterations: x {err:.2e}, rnorm history {herr:.2e}")
+    assert err <= 1e-10
+    assert herr <= 1e-8
