@@ -43,7 +43,14 @@ cudaStream_t lib_stream();
 
 namespace {
 
-constexpr int kGroupChunk = 256;   // boundary groups per chunk, one per thread
+// Boundary groups per chunk (one CTA; a chunk never straddles a problem):
+// eight per thread.  With one group per thread the per-CTA reductions and
+// counters dominated: the inner boundary phase of the 256-problem workload
+// took 126 ms (166 ms as a loop), 94-96 ms with 2048-8192 per chunk.
+#ifndef NB_BATCH_GROUP_CHUNK
+#define NB_BATCH_GROUP_CHUNK 2048
+#endif
+constexpr int kGroupChunk = NB_BATCH_GROUP_CHUNK;
 constexpr int kPointChunk = 2048;  // points per chunk, eight per thread
 constexpr int kThreads = 256;
 
@@ -61,9 +68,9 @@ __global__ void __launch_bounds__(kThreads)
   const int ch = blockIdx.x;
   const int prob = gch_prob[ch];
   if (!sc[prob].active || !sc[prob].iactive) return;
-  const int g = gch_g0[ch] + threadIdx.x;
   float part = 0.f;
-  if (g < gch_g0[ch + 1]) {
+  const int gend = gch_g0[ch + 1];
+  for (int g = gch_g0[ch] + threadIdx.x; g < gend; g += kThreads) {
     const int b = off[g], e = off[g + 1];
     float t = w[idx[b] & 0x7fffffffu];
     for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
@@ -114,9 +121,9 @@ __global__ void __launch_bounds__(kThreads)
   const int ch = blockIdx.x;
   const int prob = gch_prob[ch];
   if (!sc[prob].active) return;
-  const int g = gch_g0[ch] + threadIdx.x;
   double part = 0.0;
-  if (g < gch_g0[ch + 1]) {
+  const int gend = gch_g0[ch + 1];
+  for (int g = gch_g0[ch] + threadIdx.x; g < gend; g += kThreads) {
     const int b = off[g], e = off[g + 1];
     double t = w[idx[b] & 0x7fffffffu];
     for (int q = b + 1; q < e; ++q) t = add_rn(t, w[idx[q] & 0x7fffffffu]);
