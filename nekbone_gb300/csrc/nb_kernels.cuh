@@ -366,8 +366,14 @@ constexpr size_t ax_smem_bytes() {
 // boundary part of pap = glsc3(w,c,p) is reduced; the block that finishes
 // last adds the interior partials, forms pap and alpha = rtz1/pap (cg.f:59-61).
 // idx: member index in bits 0..30, mask flag in bit 31.
+// four resident blocks per SM (64 registers; with more registers and two
+// blocks the pass measured 0.56 ms instead of 0.40 ms, FP64 at 32^3), and
+// the launch grid is exactly the resident blocks (nb_solver.cu)
+#ifndef NB_GS_MINB
+#define NB_GS_MINB 4
+#endif
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, NB_GS_MINB)
     k_gs_fin(T *__restrict__ w, const T *__restrict__ p,
              const T *__restrict__ c, const int *__restrict__ off,
              const unsigned *__restrict__ idx, int ng,
