@@ -67,33 +67,33 @@ __device__ __forceinline__ T gs_identity() {
 template <typename T, int OP>
 __global__ void k_gs_sym(T *__restrict__ u, const int *__restrict__ off,
                          const int *__restrict__ idx, int ng) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ng) return;
-  const int b = off[g], e = off[g + 1];
-  T t = u[idx[b]];
-  for (int q = b + 1; q < e; ++q) gs_do<T, OP>(t, u[idx[q]]);
-  for (int q = b; q < e; ++q) u[idx[q]] = t;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    T t = u[idx[b]];
+    for (int q = b + 1; q < e; ++q) gs_do<T, OP>(t, u[idx[q]]);
+    for (int q = b; q < e; ++q) u[idx[q]] = t;
+  }
 }
 
 template <typename T, int OP>
 __global__ void k_gs_gather(T *__restrict__ u, const int *__restrict__ off,
                             const int *__restrict__ idx, int ng) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ng) return;
-  const int b = off[g], e = off[g + 1];
-  T t = u[idx[b]];
-  for (int q = b + 1; q < e; ++q) gs_do<T, OP>(t, u[idx[q]]);
-  u[idx[b]] = t;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    T t = u[idx[b]];
+    for (int q = b + 1; q < e; ++q) gs_do<T, OP>(t, u[idx[q]]);
+    u[idx[b]] = t;
+  }
 }
 
 template <typename T>
 __global__ void k_gs_scatter(T *__restrict__ u, const int *__restrict__ off,
                              const int *__restrict__ idx, int ng) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= ng) return;
-  const int b = off[g], e = off[g + 1];
-  const T t = u[idx[b]];
-  for (int q = b + 1; q < e; ++q) u[idx[q]] = t;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x) {
+    const int b = off[g], e = off[g + 1];
+    const T t = u[idx[b]];
+    for (int q = b + 1; q < e; ++q) u[idx[q]] = t;
+  }
 }
 
 template <typename T, int OP>
@@ -130,22 +130,51 @@ int upload_ints(const std::vector<int> &h, int **d, cudaStream_t s) {
 
 inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
+// The grid of a grid-stride gather-scatter kernel: the blocks the SMs hold
+// at once (one wave), or fewer when there are fewer groups -- the launch
+// shape that made the fused boundary pass (k_gs_fin) fastest.  For these
+// passes it measured the same as one group per thread (hsmg's V-cycle, the
+// unfused operator at 16^3).
+template <typename K>
+int resident_blocks(K kernel, int tb) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, tb, 0);
+  return std::max(1, sms) * std::max(1, per_sm);
+}
+template <typename T, int OP>
+int sym_grid(int ng) {
+  static const int cap = resident_blocks(k_gs_sym<T, OP>, 256);
+  return std::min(blocks_for(ng, 256), cap);
+}
+template <typename T, int OP>
+int gather_grid(int ng) {
+  static const int cap = resident_blocks(k_gs_gather<T, OP>, 256);
+  return std::min(blocks_for(ng, 256), cap);
+}
+template <typename T>
+int scatter_grid(int ng) {
+  static const int cap = resident_blocks(k_gs_scatter<T>, 256);
+  return std::min(blocks_for(ng, 256), cap);
+}
+
 template <typename T, int OP>
 void run_gs(const GsDevice &d, T *u, int transpose, cudaStream_t s) {
   const int TB = 256;
   if (d.symmetric) {
     if (d.ng > 0)
-      k_gs_sym<T, OP><<<blocks_for(d.ng, TB), TB, 0, s>>>(u, d.off, d.idx, d.ng);
+      k_gs_sym<T, OP><<<sym_grid<T, OP>(d.ng), TB, 0, s>>>(u, d.off, d.idx, d.ng);
     return;
   }
   const int *og = transpose ? d.off_s : d.off_g, *ig = transpose ? d.idx_s : d.idx_g;
   const int ngg = transpose ? d.ng_s : d.ng_g;
   const int *os = transpose ? d.off_g : d.off_s, *is = transpose ? d.idx_g : d.idx_s;
   const int ngs = transpose ? d.ng_g : d.ng_s;
-  if (ngg > 0) k_gs_gather<T, OP><<<blocks_for(ngg, TB), TB, 0, s>>>(u, og, ig, ngg);
+  if (ngg > 0) k_gs_gather<T, OP><<<gather_grid<T, OP>(ngg), TB, 0, s>>>(u, og, ig, ngg);
   if (!transpose && d.nfp > 0)
     k_gs_init<T, OP><<<blocks_for(d.nfp, TB), TB, 0, s>>>(u, d.fprim, d.nfp);
-  if (ngs > 0) k_gs_scatter<T><<<blocks_for(ngs, TB), TB, 0, s>>>(u, os, is, ngs);
+  if (ngs > 0) k_gs_scatter<T><<<scatter_grid<T>(ngs), TB, 0, s>>>(u, os, is, ngs);
 }
 
 template <typename T>
