@@ -9,7 +9,9 @@ runs in bench.py's cpu_check):
 * the assembled, masked operator is symmetric in the multiplicity-weighted
   inner product on continuous masked vectors, v'C(Au) = u'C(Av), to 1e-12
   relative, and positive;
-* it is linear: A(u + v/2) = Au + Av/2 to 1e-14 of max|Au|;
+* it is linear to rounding: A(u + v/2) = Au + Av/2 to 3e-14 of max|Au|
+  (three applies, each within ~5e-15 of its largest value of the exact
+  operator);
 * 100 CG iterations in the two operator forms give solutions within 1e-10
   relative and residual histories within 1e-8 relative, each decreasing by
   at least 1e3.
@@ -79,7 +81,8 @@ def test_fullsize_operator_symmetric_positive_linear(torch, case):
     s = u + 0.5 * v
     asum = _apply(torch, m, g, s, 2)
     err = float((asum - (au + 0.5 * av)).abs().max() / au.abs().max())
-    assert err <= 1e-14
+    print(f"linearity: {err:.2e}")
+    assert err <= 3e-14
 
 
 def test_fullsize_cg_operator_forms_agree(torch, case):
