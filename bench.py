@@ -52,7 +52,7 @@ UNIT = "GDOF*iter/s"
 # stream, so traffic scales with n.  Source: the profiles/ summaries named.
 DRAM_BYTES_PER_POINT = {
     1: ((531.699456e6 + 120.930048e6) / 7077888, "profiles/k_ax_eo_fp64_lx12_16cubed.md"),
-    2: ((515.452160e6 + 97.980160e6) / 7077888, "profiles/k_ax_fx_fp64_lx12_16cubed.md"),
+    2: ((511.710208e6 + 98.418944e6) / 7077888, "profiles/k_ax_fx_fp64_lx12_16cubed.md"),
 }
 RHS_SEED = 20260
 

@@ -5,8 +5,8 @@
 // GB300 executes about 0.5e12 FP64 fused multiply-adds per second, but
 // about 14e12 32x32->64-bit integer multiply-adds (mad.wide.s32) and 19e12
 // simple integer operations (measured).  A product of two 60-bit
-// fixed-point numbers built from three mad.wide.s32 therefore costs a tenth
-// of one DFMA.  So this operator keeps its values as block-floating-point
+// fixed-point numbers built from three integer multiply-adds therefore
+// costs a tenth of one DFMA.  So this operator keeps its values as block-floating-point
 // integers and leaves only the CG vector arithmetic (p update, +0.1 p, pap)
 // on the FP64 pipe:
 //
@@ -19,12 +19,15 @@
 //  * a product a*b of two such integers is formed from balanced 32-bit
 //    halves, a = ah 2^32 + al with al in [-2^31, 2^31):
 //        a*b ~= ah*bh 2^64 + (ah*bl + al*bh) 2^32,
-//    al*bl (|al*bl| <= 2^62, unbiased: al is symmetric) dropped; the terms
-//    of one output are accumulated in two int64 registers (Acc) and
-//    combined once, rounded to units of 2^64 (hh + x / 2^32: the high word
-//    of x, no shift), so one output's error is about one unit, ~2^-55 of its
-//    largest product -- the FP64 evaluation's own rounding of a 6-term sum.
-//    The rounding costs nothing: x starts at half a unit;
+//    al*bl (|al*bl| <= 2^62, unbiased: al is symmetric) dropped.  In the
+//    metric step the terms of one output are accumulated in int64 registers
+//    (Acc) and combined once, rounded to units of 2^64 (hh + x / 2^32: the
+//    high word of x, no shift; x starts at half a unit), so one output's
+//    error is about one unit, ~2^-55 of its largest product -- the FP64
+//    evaluation's own rounding of a 6-term sum.  In the six contraction
+//    stages each cross term is a 32-bit mad.hi (its high word, units of
+//    2^64) and the floors' mean loss is added back once (AccH): a few
+//    units per output, for a fifth fewer instructions;
 //  * the even-odd split of the GLL derivative (as k_ax_eo) halves the
 //    products: per point and direction 6 multiply-adds at lx1 = 12;
 //  * after the gradient and after the metric step the element's values are
