@@ -36,8 +36,9 @@
 //    element's largest value;
 //  * the result goes back to FP64 rounded to nearest even by the
 //    integer-to-FP64 conversion (one FP64-pipe operation a point) and an
-//    exact move of the exponent field; the input goes in by bit assembly
-//    (to_fixed, integer instructions only).
+//    exact move of the exponent field; the input goes in by an exact FP64
+//    scaling and the FP64-to-integer conversion (two more), where the FP64
+//    pipe has room beside the integer work.
 // This is block floating point: the error of a value is bounded relative to
 // the largest value of its element (~2^-56), where FP64 bounds it relative
 // to the value itself.  Results agree with the reference's FP64 evaluation
@@ -199,6 +200,16 @@ __device__ __forceinline__ double to_double_cvt(i64 W, int s) {
   if (d != 0.0 && e2 >= 1 && e2 <= 2046) return __longlong_as_double(b + (i64(s) << 52));
   return d == 0.0 ? 0.0 : to_double(W, s);
 }
+// x * 2^(1075 - emax + up) rounded to the nearest integer, ties to even
+// (to_fixed rounds them away from zero), by an exact FP64 scaling and the
+// FP64-to-integer conversion: two FP64-pipe operations instead of ~15
+// integer instructions (1.63 -> 1.61 ms for the operator at 32^3)
+__device__ __forceinline__ i64 to_fixed_cvt(double x, int emax, int up) {
+  const int k = 1075 - emax + up;
+  if (k > 1023 || k < -1022) return to_fixed(x, emax, up);  // 2^k not a normal double
+  const double sc = __longlong_as_double(i64(k + 1023) << 52);
+  return __double2ll_rn(x * sc);
+}
 // ----------------------------------------------------- block reductions --
 // lanes of warp w of an nt-thread block
 __device__ __forceinline__ unsigned warp_mask(int nt, int w) {
@@ -342,7 +353,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
     em = 0;
     for (int q = 0; q < (L2 + 31) / 32; ++q) em = max(em, sm.emax[q]);
 #pragma unroll
-    for (int k = 0; k < LX; ++k) sm.A[fx_at<LX>(i, j, k)] = to_fixed(uk[k], em, 6);
+    for (int k = 0; k < LX; ++k) sm.A[fx_at<LX>(i, j, k)] = to_fixed_cvt(uk[k], em, 6);
   }
   const int sP = em - 1081;  // p = P 2^sP
   __syncthreads();
