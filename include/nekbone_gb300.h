@@ -61,8 +61,8 @@ void nekbone_set_mgrid_(const int *ifmgrid);
  * 1 = even-odd split of the anti-centrosymmetric GLL derivative on the FP64
  * pipe (same result to rounding, ~27% fewer FP64 operations), 2 = the
  * even-odd form in 64-bit fixed point on the integer pipes (default: block
- * floating point, ~58 significant bits of each element's largest value;
- * same result to rounding, ~3x faster on GB300, whose FP64 pipe runs at
+ * floating point, ~55 significant bits of each element's largest value;
+ * same result to rounding, ~4x faster on GB300, whose FP64 pipe runs at
  * 1/64 of its FP32 rate).  Odd lx1 falls back to order 0; ax_e_ always uses
  * order 0. */
 void nekbone_set_contraction_order_(const int *order);

@@ -32,7 +32,7 @@
 //    products: per point and direction 6 multiply-adds at lx1 = 12;
 //  * after the gradient and after the metric step the element's values are
 //    renormalised by one shift (the element-wide OR of the magnitudes gives
-//    the top bit), so every stage works with ~58 significant bits of the
+//    the top bit), so every stage starts from ~58 significant bits of the
 //    element's largest value;
 //  * the result goes back to FP64 rounded to nearest even by the
 //    integer-to-FP64 conversion (one FP64-pipe operation a point) and an
