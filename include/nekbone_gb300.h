@@ -183,6 +183,22 @@ void nb_set_shared_metric(int on);
  * products, update); 0 (default) the fused CUDA-core iteration.  The FP64
  * defect correction is the same either way, so both reach the tolerance. */
 void nb_set_mixed_tensor_cores(int on);
+/* Mixed solver: 1 (default) the fused inner FP32 CG keeps its directions in
+ * two buffers, odd and even iterations alternating, and updates x once per
+ * two iterations (x += a_k p_k, then x += a_k+1 p_k+1, in one pass); 0 one
+ * direction buffer and an x update every iteration.  The same fused
+ * multiply-adds in the same order either way (bitwise-equal results); the
+ * first form reads and writes x half as often and takes n more floats of
+ * scratch. */
+void nb_set_mixed_paired_update(int on);
+/* Mixed solver: 1 (default) checks once per solve whether the FP32 copy of
+ * c is, bitwise at every point, a box mesh's inverse multiplicity (2^-m, m
+ * the number of the point's extreme local indices on element faces with a
+ * neighbour; even lx1 from 4 to 16), and if so the inner CG's fused
+ * iteration forms c instead of reading it (4 bytes a point less in the
+ * update, the interior's c = 1 not read by the operator); 0 always reads c.
+ * The same values either way (bitwise-equal results). */
+void nb_set_mixed_closed_multiplicity(int on);
 /* The mesh's gather-scatter groups (jl order: groups by primary, members
  * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)
  * are filled when given. */

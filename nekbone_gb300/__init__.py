@@ -59,6 +59,7 @@ EXPORTS = (
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
+    "nb_set_mixed_paired_update", "nb_set_mixed_closed_multiplicity",
     "nb_wait_selftest", "nb_set_wait_test", "nb_pipe_rates",
 )
 
@@ -132,6 +133,10 @@ lib.nb_set_shared_metric.restype = None
 lib.nb_set_shared_metric.argtypes = [_i]
 lib.nb_set_mixed_tensor_cores.restype = None
 lib.nb_set_mixed_tensor_cores.argtypes = [_i]
+lib.nb_set_mixed_paired_update.restype = None
+lib.nb_set_mixed_paired_update.argtypes = [_i]
+lib.nb_set_mixed_closed_multiplicity.restype = None
+lib.nb_set_mixed_closed_multiplicity.argtypes = [_i]
 lib.nb_wait_selftest.restype = _i
 lib.nb_wait_selftest.argtypes = [_C.c_uint]
 lib.nb_set_wait_test.restype = _i
@@ -671,6 +676,20 @@ def set_mixed_tensor_cores(on: bool) -> None:
     """Mixed solver: the inner CG's element products on the tensor cores
     (True) or the fused CUDA-core iteration (False, default)."""
     lib.nb_set_mixed_tensor_cores(1 if on else 0)
+
+
+def set_mixed_paired_update(on: bool) -> None:
+    """Mixed solver: the inner FP32 CG's x updated once per two iterations
+    from two direction buffers (True, default) or every iteration (False);
+    bitwise the same iterates."""
+    lib.nb_set_mixed_paired_update(1 if on else 0)
+
+
+def set_mixed_closed_multiplicity(on: bool) -> None:
+    """Mixed solver: the inner FP32 CG forms c in closed form when c
+    verifies as a box mesh's inverse multiplicity (True, default), or
+    always reads it (False); bitwise the same iterates."""
+    lib.nb_set_mixed_closed_multiplicity(1 if on else 0)
 
 
 def set_shared_metric(on: bool) -> None:

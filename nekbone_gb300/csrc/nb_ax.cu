@@ -21,6 +21,7 @@ int launch_ax_fx_m2(const Operator &op, AxArgs<double> a, cudaStream_t s);
 template <>
 int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream_t s) {
   a.nelt = op.nelt;
+  if (!a.pold) a.pold = a.p;  // MODE 1 reads the old direction from pold
   a.err = device_error_word();
   a.wait_test = wait_test_mode();
   if (op.order == 2 && op.fx_ok) {  // fixed point on the integer pipes
@@ -44,6 +45,7 @@ int launch_ax<double>(const Operator &op, int mode, AxArgs<double> a, cudaStream
 template <>
 int launch_ax<float>(const Operator &op, int mode, AxArgs<float> a, cudaStream_t s) {
   a.nelt = op.nelt;
+  if (!a.pold) a.pold = a.p;  // MODE 1 reads the old direction from pold
   a.err = device_error_word();
   a.wait_test = wait_test_mode();
   if (op.order >= 1 && op.eo_ok && mode != 2) {  // even-odd, one line per thread

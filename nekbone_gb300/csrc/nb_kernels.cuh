@@ -88,6 +88,7 @@ __device__ __forceinline__ bool last_block(unsigned *counter, int nblocks) {
 struct CgScalars {
   double rtz1, rtz2, beta, pap, alpha, rtr, rnorm;
   double rtr_first;  // rtr of iteration 1 (cg.f:68)
+  double alpha_prev;  // alpha of the iteration whose x update was deferred
   int iter;
   int pad;
 };
@@ -107,6 +108,10 @@ struct AxArgs {
   T *w;
   const T *u;        // MODE 0 input; MODE 1: z
   T *p;              // MODE 1: search direction (read old, write new); MODE 2: x
+  const T *pold;     // MODE 1: the old direction, read from here (another
+                     //   buffer than p when the directions alternate; launch_ax
+                     //   sets it to p when null: a select of the two pointers
+                     //   in the kernel measured 25 % slower, FP32 at 32^3)
   const T *g;        // gxyz(6, nxyz, nelt)
   const T *c;        // MODE 1/2: inverse multiplicity
   const T *D;        // dxm1(lx1,lx1) column-major: D(i,m) at D[i + m*lx1]
@@ -126,6 +131,8 @@ struct AxArgs {
   const int *el_prob;  // fixed-point operator in a batched solve: element e is
   const int *act;      //   skipped when act[el_prob[e] * act_stride] is 0 (its
   int act_stride;      //   problem is no longer active); null for one mesh
+  int c_unit_interior;  // MODE 1: c is 1 at every element-interior point (a
+                        //   verified multiplicity): not read there
 };
 
 template <typename T, int LX>
@@ -205,7 +212,7 @@ __global__ void __launch_bounds__(LX * LX)
 #pragma unroll
     for (int k = 1; k < LX - 1; ++k) {
       const size_t id = base + size_t(k) * L2 + tid;
-      creg[k] = a.c[id];
+      creg[k] = (MODE == 1 && a.c_unit_interior) ? T(1) : a.c[id];
       if (MODE == 2) freg[k] = a.f[id];
     }
   }
@@ -220,7 +227,7 @@ __global__ void __launch_bounds__(LX * LX)
     const size_t id = base + size_t(k) * L2 + tid;
     if (MODE == 1) {
       ureg[k] = a.u[id];
-      pold[k] = a.first ? T(0) : a.p[id];
+      pold[k] = a.first ? T(0) : a.pold[id];
     } else if (MODE == 2) {
       ureg[k] = a.p[id];
       pold[k] = a.e ? T(a.e[id]) : T(0);
@@ -499,16 +506,32 @@ __global__ void __launch_bounds__(256)
 // x += alpha p; r -= alpha w (add2s2, cg.f:63-64); rtr = glsc3(r,c,r) (cg.f:66).
 // The last block forms rnorm and, for the identity preconditioner (z = r),
 // the next rtz1 = rtr and beta = rtz1/rtz2 (cg.f:52-55).
-template <typename T>
+// DEFER pairs the x updates of two iterations whose directions sit in two
+// buffers: 1 leaves x alone and keeps alpha in sc->alpha_prev; 2 then makes
+// x += alpha_prev pprev, x += alpha p, the two fused multiply-adds of the
+// unpaired form in the same order (bitwise the same x), reading and writing
+// x once for the two iterations.
+// CF (FP32, even lx <= 16): c is the verified closed-form multiplicity
+// (c_closed_form), 2^-m with m the number of the point's extreme local
+// indices whose face has a neighbour (cface[e]: bit 0/1 the faces i = 0 /
+// lx-1, 2/3 for j, 4/5 for k); the 16-byte path forms it instead of
+// reading c (the same values, so the same rtr).
+template <typename T, int DEFER = 0, bool CF = false>
 __global__ void __launch_bounds__(256)
     k_cg_update(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
                 const T *__restrict__ w, const T *__restrict__ c, long n,
                 double *__restrict__ partial, unsigned *counter, CgScalars *sc,
                 double *hist, int iter, int identity_precond,
-                float *__restrict__ r32 = nullptr) {
+                float *__restrict__ r32 = nullptr, const T *__restrict__ pprev = nullptr,
+                const unsigned char *__restrict__ cface = nullptr, int lx = 0) {
   __shared__ double red[32];
+  // CF: the extreme-index bits of the four points of each 16-byte group
+  // of an element, one byte a point
+  __shared__ unsigned ext4[CF ? 1024 : 1];
   const T alpha = T(sc->alpha);
   const T alphm = -alpha;
+  const T alpha0 = DEFER == 2 ? T(sc->alpha_prev) : T(0);
+  if (DEFER == 1 && blockIdx.x == 0 && threadIdx.x == 0) sc->alpha_prev = sc->alpha;
   T part = T(0);
   // 16-byte loads and stores (two doubles or four floats a thread) when
   // every vector allows them
@@ -516,27 +539,72 @@ __global__ void __launch_bounds__(256)
   typedef typename std::conditional<sizeof(T) == 8, double2, float4>::type V;
   const uintptr_t al = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
                        reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(w) |
-                       reinterpret_cast<uintptr_t>(c);
+                       reinterpret_cast<uintptr_t>(c) |
+                       (DEFER == 2 ? reinterpret_cast<uintptr_t>(pprev) : uintptr_t(0));
   const bool vec = (al & 15u) == 0 && n % VEC == 0 &&
                    (!r32 || (reinterpret_cast<uintptr_t>(r32) & uintptr_t(4 * VEC - 1)) == 0);
+  // CF: element e and group l4 of v, advanced by the stride's quotient and
+  // remainder
+  long e = 0, se = 0;
+  int l4 = 0, sl = 0;
+  const int Q = CF ? lx * lx * lx / 4 : 1;
+  if constexpr (CF) {
+    const long v0 = long(blockIdx.x) * blockDim.x + threadIdx.x;
+    const long vs = long(gridDim.x) * blockDim.x;
+    static_assert(VEC == 4, "closed-form multiplicity: FP32 only");
+    const int L2 = lx * lx;
+    for (int t = threadIdx.x; t < Q; t += blockDim.x) {
+      unsigned b4 = 0;
+      for (int d = 0; d < 4; ++d) {
+        const int l = 4 * t + d, i = l % lx, j = (l / lx) % lx, k = l / L2;
+        const unsigned b = (i == 0 ? 1u : 0u) | (i == lx - 1 ? 2u : 0u) |
+                           (j == 0 ? 4u : 0u) | (j == lx - 1 ? 8u : 0u) |
+                           (k == 0 ? 16u : 0u) | (k == lx - 1 ? 32u : 0u);
+        b4 |= b << (8 * d);
+      }
+      ext4[t] = b4;
+    }
+    __syncthreads();
+    e = v0 / Q;
+    l4 = int(v0 - e * Q);
+    se = vs / Q;
+    sl = int(vs - se * Q);
+  }
   if (vec) {
     for (long v = long(blockIdx.x) * blockDim.x + threadIdx.x; v < n / VEC;
          v += long(gridDim.x) * blockDim.x) {
-      alignas(16) T xa[VEC], ra[VEC], pa[VEC], wa[VEC], ca[VEC];
-      *reinterpret_cast<V *>(xa) = reinterpret_cast<const V *>(x)[v];
+      alignas(16) T xa[VEC], ra[VEC], pa[VEC], wa[VEC], ca[VEC], qa[VEC];
+      if (DEFER != 1) {
+        *reinterpret_cast<V *>(xa) = reinterpret_cast<const V *>(x)[v];
+        *reinterpret_cast<V *>(pa) = reinterpret_cast<const V *>(p)[v];
+      }
+      if (DEFER == 2) *reinterpret_cast<V *>(qa) = reinterpret_cast<const V *>(pprev)[v];
       *reinterpret_cast<V *>(ra) = reinterpret_cast<const V *>(r)[v];
-      *reinterpret_cast<V *>(pa) = reinterpret_cast<const V *>(p)[v];
       *reinterpret_cast<V *>(wa) = reinterpret_cast<const V *>(w)[v];
-      *reinterpret_cast<V *>(ca) = reinterpret_cast<const V *>(c)[v];
+      if constexpr (CF) {
+        const unsigned fb = __ldg(cface + e), b4 = ext4[l4];
+#pragma unroll
+        for (int q = 0; q < VEC; ++q)
+          ca[q] = T(__int_as_float((127 - __popc((b4 >> (8 * q)) & fb)) << 23));
+        l4 += sl;
+        e += se;
+        if (l4 >= Q) {
+          l4 -= Q;
+          ++e;
+        }
+      } else {
+        *reinterpret_cast<V *>(ca) = reinterpret_cast<const V *>(c)[v];
+      }
       alignas(16) float r3[VEC];
 #pragma unroll
       for (int q = 0; q < VEC; ++q) {
-        xa[q] = fma_rn(alpha, pa[q], xa[q]);
+        if (DEFER == 2) xa[q] = fma_rn(alpha0, qa[q], xa[q]);
+        if (DEFER != 1) xa[q] = fma_rn(alpha, pa[q], xa[q]);
         ra[q] = fma_rn(alphm, wa[q], ra[q]);
         r3[q] = float(ra[q]);
         part = fma_rn(mul_rn(ra[q], ca[q]), ra[q], part);
       }
-      reinterpret_cast<V *>(x)[v] = *reinterpret_cast<const V *>(xa);
+      if (DEFER != 1) reinterpret_cast<V *>(x)[v] = *reinterpret_cast<const V *>(xa);
       reinterpret_cast<V *>(r)[v] = *reinterpret_cast<const V *>(ra);
       if (r32) {
         if constexpr (VEC == 2)
@@ -548,7 +616,8 @@ __global__ void __launch_bounds__(256)
   } else {
     for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n;
          q += long(gridDim.x) * blockDim.x) {
-      x[q] = fma_rn(alpha, p[q], x[q]);
+      if (DEFER == 2) x[q] = fma_rn(alpha, p[q], fma_rn(alpha0, pprev[q], x[q]));
+      else if (DEFER == 0) x[q] = fma_rn(alpha, p[q], x[q]);
       const T rv = fma_rn(alphm, w[q], r[q]);
       r[q] = rv;
       if (r32) r32[q] = float(rv);  // the FP32 V-cycle's input, as k_to_f32 makes it
@@ -710,7 +779,8 @@ __global__ void __launch_bounds__(LX * LX)
   float creg[LX];
   if (MODE == 1 && col_interior) {
 #pragma unroll
-    for (int k = 1; k < LX - 1; ++k) creg[k] = a.c[base + size_t(k) * L2 + tid];
+    for (int k = 1; k < LX - 1; ++k)
+      creg[k] = a.c_unit_interior ? 1.f : a.c[base + size_t(k) * L2 + tid];
   }
   float beta = 0.f;
   if (MODE == 1 && !a.first) beta = float(a.sc->beta);
@@ -719,7 +789,7 @@ __global__ void __launch_bounds__(LX * LX)
   for (int k = 0; k < LX; ++k) {  // all loads before the first store
     const size_t id = base + size_t(k) * L2 + tid;
     ureg[k] = a.u[id];
-    pold[k] = (MODE == 1 && !a.first) ? a.p[id] : 0.f;
+    pold[k] = (MODE == 1 && !a.first) ? a.pold[id] : 0.f;
   }
 #pragma unroll
   for (int k = 0; k < LX; ++k) {
@@ -979,7 +1049,7 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
 #pragma unroll
     for (int k = 1; k < LX - 1; ++k) {
       const size_t id = base + size_t(k) * L2 + t;
-      creg[k] = a.c[id];
+      creg[k] = (MODE == 1 && a.c_unit_interior) ? T(1) : a.c[id];
       if (MODE == 2) freg[k] = a.f[id];
     }
   }
@@ -990,7 +1060,7 @@ __device__ __forceinline__ void ax_eo_body(const AxArgs<T> &a, const EoCoef<T, L
     const size_t id = base + size_t(k) * L2 + t;
     if (MODE == 1) {
       ureg[k] = a.u[id];
-      pold[k] = a.first ? T(0) : a.p[id];
+      pold[k] = a.first ? T(0) : a.pold[id];
     } else if (MODE == 2) {
       ureg[k] = a.p[id];
       pold[k] = a.e ? T(a.e[id]) : T(0);

@@ -208,6 +208,12 @@ void set_shared_metric(bool on) { g_shared_metric = on; }
 // the inner CG's element products on the tensor cores (k_ax_tc: FP16 hi+lo
 // split operands, FP32 accumulation) instead of the fused CUDA-core pass
 bool g_mixed_tc = false;
+// the inner CG's x updated once per two iterations from two direction
+// buffers (cg_device_f32's p_alt; bitwise the same iterates)
+bool g_mixed_paired = true;
+// the inner CG forms c in closed form where c verifies as a box mesh's
+// inverse multiplicity (c_closed_form; the same values)
+bool g_mixed_closed_c = true;
 
 // flag: one device int of scratch
 int metric_uniform(const float *g32, long nelt, int lx, int *flag, int *uniform,
@@ -235,6 +241,8 @@ extern "C" {
 
 void nb_set_shared_metric(int on) { set_shared_metric(on != 0); }
 void nb_set_mixed_tensor_cores(int on) { g_mixed_tc = on != 0; }
+void nb_set_mixed_paired_update(int on) { g_mixed_paired = on != 0; }
+void nb_set_mixed_closed_multiplicity(int on) { g_mixed_closed_c = on != 0; }
 
 int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
                 const double *c, double tol, int inner_iters, int max_outer,
@@ -247,23 +255,29 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
   cudaStream_t s = lib_stream();
   const long n = op.n;
   // reduction buffers (this may be the mesh's first solve), then scratch:
-  // r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32 (FP32); one int flag
+  // r, w (FP64); g32 (6n), c32, r32, e32, rr32, w32, p32, p32b (FP32); two
+  // int flags; the elements' face bits (nelt bytes)
   int st = wk.ensure(op, std::max(inner_iters, 1));
   metric_fx_invalidate(op);
-  if (!st) st = wk.ensure_scratch(size_t(n) * (2 * 8 + 12 * 4) + 16);
+  const size_t flags_at = size_t(n) * (2 * 8 + 13 * 4);
+  if (!st) st = wk.ensure_scratch(flags_at + 16 + size_t(op.nelt));
   if (st) return st;
   double *r = reinterpret_cast<double *>(wk.scratch);
   double *w = r + n;
   float *g32 = reinterpret_cast<float *>(w + n);
   float *c32 = g32 + 6 * n, *r32 = c32 + n, *e32 = r32 + n, *rr32 = e32 + n,
-        *w32 = rr32 + n, *p32 = w32 + n;
+        *w32 = rr32 + n, *p32 = w32 + n, *p32b = p32 + n;
   int k = 0, inner = 0;
   double rn0 = 0.0, rn = 0.0;
   if (!st) st = vec_convert<float, double>(g32, g, 6 * n, s);
   if (!st) st = vec_convert<float, double>(c32, c, n, s);
   int uniform = 0;
-  int *flag = reinterpret_cast<int *>(wk.scratch + size_t(n) * (2 * 8 + 12 * 4));
+  int *flag = reinterpret_cast<int *>(wk.scratch + flags_at);
+  unsigned char *cface = wk.scratch + flags_at + 16;
+  bool closed = false;
   if (!st) st = metric_uniform(g32, op.nelt, op.lx, flag, &uniform, s);
+  if (!st && g_mixed_closed_c && op.fused_ok && !g_mixed_tc)
+    st = c_closed_form(op, c32, cface, flag + 1, &closed, s);
   // x = 0, r = mask(f)
   if (!st && cudaMemsetAsync(x, 0, n * 8, s) != cudaSuccess) st = fail(NB_ERR_CUDA, "memset");
   if (!st) st = vec_copy<double>(r, f, n, s);
@@ -285,9 +299,13 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     st = dev_scale_to_f32(r32, r, 1.0 / rn, n, s);
     wk.g32_uniform = uniform;
     wk.tc_inner = g_mixed_tc;
-    if (!st) st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s);
+    wk.c32_face = closed ? cface : nullptr;
+    if (!st)
+      st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s,
+                         g_mixed_paired ? p32b : nullptr);
     wk.g32_uniform = 0;
     wk.tc_inner = false;
+    wk.c32_face = nullptr;
     // FP64 defect: x += |r| e; r = f - A x; r'Cr
     if (!st && fused) {
       st = residual_fused(op, wk, x, e32, rn, f, g, c, r, w, s);

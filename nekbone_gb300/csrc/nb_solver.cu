@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 
 #include "nb_solver.h"
 
@@ -470,6 +471,80 @@ int grid_for(long n) {
   return int(std::max(1L, std::min<long>(long(sm_count()) * 8, (n + 255) / 256)));
 }
 
+// Each element's face bits (cface: bit 0/1 the faces i = 0 / lx-1 have a
+// neighbour, 2/3 for j, 4/5 for k; read from c at the face points (1,1),
+// 1/2 with a neighbour), and *ok cleared when any point's c differs
+// bitwise from 2^-m, m the number of its extreme local indices on faces
+// with a neighbour (lx >= 3).  One block per element at a time.
+__global__ void k_c_closed_form(const float *__restrict__ c, int lx, long nelt,
+                                unsigned char *__restrict__ cface, int *ok) {
+  __shared__ unsigned fb_s;
+  const int L2 = lx * lx, L3 = L2 * lx;
+  for (long e = blockIdx.x; e < nelt; e += gridDim.x) {
+    const float *ce = c + e * L3;
+    if (threadIdx.x == 0) {
+      const int m = 1, h = lx - 1;
+      const int pt[6] = {0 + lx * m + L2 * m, h + lx * m + L2 * m, m + 0 + L2 * m,
+                         m + lx * h + L2 * m, m + lx * m + 0,  m + lx * m + L2 * h};
+      unsigned fb = 0;
+      for (int f = 0; f < 6; ++f)
+        if (ce[pt[f]] == 0.5f) fb |= 1u << f;
+      fb_s = fb;
+      cface[e] = (unsigned char)fb;
+    }
+    __syncthreads();
+    const unsigned fb = fb_s;
+    bool good = true;
+    for (int l = threadIdx.x; l < L3; l += blockDim.x) {
+      const int i = l % lx, j = (l / lx) % lx, k = l / L2;
+      const unsigned b = (i == 0 ? 1u : 0u) | (i == lx - 1 ? 2u : 0u) | (j == 0 ? 4u : 0u) |
+                         (j == lx - 1 ? 8u : 0u) | (k == 0 ? 16u : 0u) |
+                         (k == lx - 1 ? 32u : 0u);
+      const unsigned want = unsigned(127 - __popc(b & fb)) << 23;
+      good &= __float_as_uint(ce[l]) == want;
+    }
+    // (also keeps the next element's fb_s write behind every read of this one)
+    if (!__syncthreads_and(good) && threadIdx.x == 0) atomicExch(ok, 0);
+  }
+}
+
+}  // namespace
+
+int c_closed_form(const Operator &op, const float *c32, unsigned char *cface, int *flag,
+                  bool *closed, cudaStream_t s) {
+  *closed = false;
+  if (op.lx % 2 != 0 || op.lx < 4 || op.lx > 16 || op.nelt < 1) return NB_OK;
+  const int one = 1;
+  int h = 0;
+  NB_CUDA(cudaMemcpyAsync(flag, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+  const int grid = int(std::min<long>(op.nelt, long(sm_count()) * 8));
+  k_c_closed_form<<<grid, 256, 0, s>>>(c32, op.lx, op.nelt, cface, flag);
+  NB_CUDA(cudaGetLastError());
+  NB_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  NB_CUDA(cudaStreamSynchronize(s));
+  *closed = h != 0;
+  return NB_OK;
+}
+
+namespace {
+// k_cg_update with pairing mode D; FP32 forms c in closed form when the
+// solve in progress verified it (wk.c32_face)
+template <typename T, int D>
+void update_launch(const Operator &op, const CgWork &wk, T *x, T *r, const T *p,
+                   const T *w, const T *c, double *hist, int iter, int identity,
+                   float *r32, const T *pprev, cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (wk.c32_face) {
+      k_cg_update<T, D, true><<<wk.grid_up, 256, 0, s>>>(
+          x, r, p, w, c, op.n, wk.partial_up, wk.counters + 1, wk.sc, hist, iter, identity,
+          r32, pprev, wk.c32_face, op.lx);
+      return;
+    }
+  }
+  k_cg_update<T, D><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, op.n, wk.partial_up,
+                                               wk.counters + 1, wk.sc, hist, iter, identity,
+                                               r32, pprev);
+}
 }  // namespace
 
 template <typename T>
@@ -582,16 +657,27 @@ static int cg_begin_t(Operator &op, CgWork &wk, T *x, const T *f, const T *c,
   return vec_glsc3<T>(r, c, r, n, wk, wk.dot_out, wk.sc, 1, 0, s);
 }
 
-// iterations it0..it1 of cg.f:48-75
+// iterations it0..it1 of cg.f:48-75.  With p_alt (the fused FP32 inner CG
+// from its first iteration), the directions of odd iterations go to p and
+// those of even iterations to p_alt, and each pair of iterations updates x
+// once (k_cg_update DEFER 1, then 2).
 template <typename T>
 static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
                       T *r, T *w, T *p, T *z, int it0, int it1, int niter,
-                      Precond *M, bool force_unfused, cudaStream_t s) {
+                      Precond *M, bool force_unfused, cudaStream_t s,
+                      T *p_alt = nullptr) {
   const long n = op.n;
   const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
   const bool tc = std::is_same<T, float>::value && wk.tc_inner;
   const bool fused = op.fused_ok && !force_unfused && !tc;
+  const bool paired = p_alt && fused && !M && it0 == 1;
+  T *const p_odd = p;
   for (int iter = it0; iter <= it1; ++iter) {
+    T *pold = nullptr;
+    if (paired) {
+      p = (iter & 1) ? p_odd : p_alt;
+      pold = (iter & 1) ? p_alt : p_odd;
+    }
     T *zz = r;
     if (M) {
       if (!std::is_same<T, double>::value)
@@ -622,6 +708,8 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
       a.sc = wk.sc;
       a.partial = wk.partial_ax;
       a.first = iter == 1;
+      a.pold = iter == 1 ? nullptr : pold;
+      a.c_unit_interior = std::is_same<T, float>::value && wk.c32_face ? 1 : 0;
       a.g_uniform = std::is_same<T, float>::value ? wk.g32_uniform : 0;
       NB_TRY(launch_ax<T>(op, 1, a, s));
       k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx,
@@ -644,10 +732,13 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
       NB_CUDA(cudaGetLastError());
     }
     float *r32 = M ? M->r32_in() : nullptr;
-    k_cg_update<T><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, n, wk.partial_up,
-                                              wk.counters + 1, wk.sc,
-                                              iter < wk.hist_len ? wk.hist : nullptr,
-                                              iter, M == nullptr, r32);
+    double *hist = iter < wk.hist_len ? wk.hist : nullptr;
+    if (paired && (iter & 1) && iter < it1)
+      update_launch<T, 1>(op, wk, x, r, p, w, c, hist, iter, 1, nullptr, nullptr, s);
+    else if (paired && !(iter & 1))
+      update_launch<T, 2>(op, wk, x, r, p, w, c, hist, iter, 1, nullptr, pold, s);
+    else
+      update_launch<T, 0>(op, wk, x, r, p, w, c, hist, iter, M == nullptr, r32, nullptr, s);
     wk.r32_ready = r32 != nullptr;
     NB_CUDA(cudaGetLastError());
   }
@@ -683,31 +774,66 @@ template <typename T>
 int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
                       const T *c, T *r, T *w, T *p, int reps, double *ms3,
                       cudaStream_t s) {
-  NB_TRY(cg_begin_t<T>(op, wk, x, f, c, r, true, reps + 2, s));
+  // FP32: the mixed solver's inner CG form, directions alternating between
+  // p and a second buffer, x updated once per pair of iterations, and c
+  // formed in closed form where it verifies
+  constexpr bool PAIRED = std::is_same<T, float>::value;
+  const int iters = PAIRED ? 2 * reps : reps;
+  T *p_alt = nullptr;
+  unsigned char *cface = nullptr;
+  if (PAIRED) {
+    NB_CUDA(cudaMalloc(&p_alt, op.n * sizeof(T)));
+    NB_CUDA(cudaMalloc(&cface, size_t(op.nelt) + 16));
+  }
+  std::unique_ptr<T, int (*)(T *)> p_alt_owner(p_alt, [](T *q) { return int(cudaFree(q)); });
+  std::unique_ptr<unsigned char, int (*)(unsigned char *)> cface_owner(
+      cface, [](unsigned char *q) { return int(cudaFree(q)); });
+  struct FaceReset {
+    CgWork &wk;
+    ~FaceReset() { wk.c32_face = nullptr; }
+  } face_reset{wk};
+  if constexpr (PAIRED) {
+    bool closed = false;
+    int *flag = reinterpret_cast<int *>(cface + ((size_t(op.nelt) + 3) & ~size_t(3)));
+    NB_TRY(c_closed_form(op, (const float *)c, cface, flag, &closed, s));
+    wk.c32_face = closed ? cface : nullptr;
+  }
+  NB_TRY(cg_begin_t<T>(op, wk, x, f, c, r, true, iters + 2, s));
   NB_TRY(cg_steps_t<T>(op, wk, x, g, c, r, w, p, r, 1, 1, -1, nullptr, false, s));
   cudaEvent_t ev[4];
   for (auto &e : ev) NB_CUDA(cudaEventCreate(&e));
   double acc[3] = {0, 0, 0};
   const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
-  for (int it = 0; it < reps; ++it) {
+  for (int it = 0; it < iters; ++it) {
+    // iteration it + 2; pairs (2,3), (4,5), ...: the first of a pair writes
+    // its direction to p_alt and defers its x update
+    const bool first_of_pair = PAIRED && (it & 1) == 0;
+    T *pc = first_of_pair ? p_alt : p;
+    const T *po = !PAIRED ? nullptr : first_of_pair ? p : p_alt;
     AxArgs<T> a{};
     a.w = w;
     a.u = r;
-    a.p = p;
+    a.p = pc;
+    a.pold = po;
     a.g = g;
     a.c = c;
+    a.c_unit_interior = wk.c32_face ? 1 : 0;
     a.D = D;
     a.sc = wk.sc;
     a.partial = wk.partial_ax;
     NB_CUDA(cudaEventRecord(ev[0], s));
     NB_TRY(launch_ax<T>(op, 1, a, s));
     NB_CUDA(cudaEventRecord(ev[1], s));
-    k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, p, c, op.bnd_off, op.bnd_idx, op.nbg,
+    k_gs_fin<T><<<wk.grid_gs, 256, 0, s>>>(w, pc, c, op.bnd_off, op.bnd_idx, op.nbg,
                                            wk.partial_gs, wk.partial_ax, op.nelt,
                                            wk.counters + 0, wk.sc);
     NB_CUDA(cudaEventRecord(ev[2], s));
-    k_cg_update<T><<<wk.grid_up, 256, 0, s>>>(x, r, p, w, c, op.n, wk.partial_up,
-                                              wk.counters + 1, wk.sc, nullptr, it + 2, 1);
+    if (!PAIRED)
+      update_launch<T, 0>(op, wk, x, r, pc, w, c, nullptr, it + 2, 1, nullptr, nullptr, s);
+    else if (first_of_pair)
+      update_launch<T, 1>(op, wk, x, r, pc, w, c, nullptr, it + 2, 1, nullptr, nullptr, s);
+    else
+      update_launch<T, 2>(op, wk, x, r, pc, w, c, nullptr, it + 2, 1, nullptr, po, s);
     NB_CUDA(cudaEventRecord(ev[3], s));
     NB_CUDA(cudaEventSynchronize(ev[3]));
     for (int k = 0; k < 3; ++k) {
@@ -717,7 +843,7 @@ int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
     }
   }
   for (auto &e : ev) cudaEventDestroy(e);
-  for (int k = 0; k < 3; ++k) ms3[k] = acc[k] / (reps > 0 ? reps : 1);
+  for (int k = 0; k < 3; ++k) ms3[k] = acc[k] / (iters > 0 ? iters : 1);
   return NB_OK;
 }
 template int time_cg_kernels_t<double>(Operator &, CgWork &, double *, const double *,
@@ -775,10 +901,10 @@ int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
 
 int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
                   const float *g, const float *c, float *r, float *w, float *p,
-                  int niter, cudaStream_t s) {
+                  int niter, cudaStream_t s, float *p_alt) {
   NB_TRY(cg_begin_t<float>(op, wk, x, f, c, r, true, niter, s));
   return cg_steps_t<float>(op, wk, x, g, c, r, w, p, r, 1, niter, niter,
-                           nullptr, false, s);
+                           nullptr, false, s, p_alt);
 }
 
 }  // namespace nb

@@ -85,6 +85,10 @@ struct CgWork {
   // an FP32 solve in progress takes its element products on the tensor
   // cores (unfused iteration; set by the mixed solver around its inner CG)
   bool tc_inner = false;
+  // an FP32 solve in progress whose c verified as the closed-form
+  // multiplicity (c_closed_form): each element's face bits; the fused
+  // iteration then forms c instead of reading it (same values)
+  const unsigned char *c32_face = nullptr;
   ~CgWork();
   int ensure(const Operator &op, int niter);
   int ensure_scratch(size_t bytes);
@@ -202,7 +206,8 @@ int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
 int residual_fused(Operator &op, CgWork &wk, double *x, const float *e,
                    double scale, const double *f, const double *g,
                    const double *c, double *r, double *w, cudaStream_t s);
-// CUDA-event times of the three kernels of a fused CG iteration
+// CUDA-event times of the three kernels of a fused CG iteration (FP32: the
+// average over a pair of iterations with the paired x update)
 template <typename T>
 int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
                       const T *c, T *r, T *w, T *p, int reps, double *ms3,
@@ -217,9 +222,19 @@ int launch_cg_update(const Operator &op, CgWork &wk, double *x, double *r,
 int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
                 const double *c, double *r, double *w, double *p, double *z,
                 int it0, int it1, Precond *M, cudaStream_t s);
+// Whether the FP32 c is, bitwise at every point, 2^-m with m the number of
+// the point's extreme local indices whose element face has a neighbour (a
+// box mesh's inverse multiplicity): then *closed and cface[e] holds element
+// e's face bits (bit 0/1 the faces i = 0 / lx-1, 2/3 for j, 4/5 for k).
+// Even lx1 from 4 to 16 only.  flag: one device int; synchronises s.
+int c_closed_form(const Operator &op, const float *c32, unsigned char *cface, int *flag,
+                  bool *closed, cudaStream_t s);
 // FP32 variant (inner solves of the mixed-precision path), x starts at 0.
+// With p_alt (a second n-point direction buffer) the fused iterations
+// alternate their directions between p and p_alt and update x once per two
+// iterations (bitwise the same iterates, 8 fewer bytes a point per pair).
 int cg_device_f32(Operator &op, CgWork &wk, float *x, const float *f,
                   const float *g, const float *c, float *r, float *w, float *p,
-                  int niter, cudaStream_t s);
+                  int niter, cudaStream_t s, float *p_alt = nullptr);
 
 }  // namespace nb

@@ -379,6 +379,79 @@ def test_mixed_shared_metric_bitwise(nb, deformed):
     assert np.array_equal(xs[True][0], xs[False][0])
 
 
+@pytest.mark.parametrize("lx,inner,mask", [(10, 20, 1), (10, 7, 1), (7, 20, 1), (8, 20, 0)])
+def test_mixed_inner_forms_bitwise(nb, lx, inner, mask):
+    """The inner FP32 CG's streamlined forms give bitwise the solution and
+    cycle count of the plain one: two direction buffers with one x update
+    per pair of iterations (an odd inner count leaves its last iteration
+    unpaired; odd lx1 takes the general operator), and c formed in closed
+    form after it verified as the box's inverse multiplicity (even lx1; in
+    either mask mode, since c does not depend on the mask).  Mask mode 0
+    (the reference's element-1 quirk leaves most of the boundary free) is
+    compared over six outer cycles, without a tolerance to reach."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(5, 4, 3, lx, mask_mode=mask)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g_deformed(g.data_ptr(), 5, 0.1)
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 13)
+    # mask mode 0 masks every domain face on the mesh's first masking and
+    # element 1's list after it (maskit's first-call branch): one solve
+    # first, so that every compared solve sees the same mask
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(), 1e-10, inner, 1)
+    xs = {}
+    try:
+        for paired, closed in ((True, True), (False, True), (True, False), (False, False)):
+            nb.set_mixed_paired_update(paired)
+            nb.set_mixed_closed_multiplicity(closed)
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            outer, tot, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(),
+                                        c.data_ptr(), 1e-10, inner, 500 if mask else 6)
+            assert rr <= 1e-10 or not mask
+            xs[paired, closed] = (x.cpu().numpy(), outer, rr)
+    finally:
+        nb.set_mixed_paired_update(True)
+        nb.set_mixed_closed_multiplicity(True)
+    ref = xs[False, False]
+    for key, got in xs.items():
+        assert got[1:] == ref[1:], key
+        assert np.array_equal(got[0], ref[0]), key
+
+
+def test_mixed_closed_multiplicity_rejects_other_c(nb):
+    """A c that is not the box's inverse multiplicity (one point changed)
+    fails the closed-form check, and the inner CG reads it: the solve
+    equals the one with the closed form switched off."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(4, 3, 3, 8, mask_mode=1)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g(g.data_ptr())
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 17)
+    c[8 ** 3 * 5 + 4 + 8 * 3 + 64 * 2] = 0.75   # point (4,3,2) of element 5: interior
+    xs = []
+    try:
+        for closed in (True, False):
+            nb.set_mixed_closed_multiplicity(closed)
+            x = torch.zeros(n, dtype=torch.float64, device=dev)
+            outer, tot, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(),
+                                        c.data_ptr(), 1e-9, 20, 60)
+            xs.append((x.cpu().numpy(), outer, rr))
+    finally:
+        nb.set_mixed_closed_multiplicity(True)
+    assert xs[0][1:] == xs[1][1:]
+    assert np.array_equal(xs[0][0], xs[1][0])
+
+
 # -------------------------------------------------------------------- hsmg --
 @pytest.mark.parametrize("nx", [4, 5, 8, 10])
 def test_h1mg_solve_matches_oracle(nb, nx):
