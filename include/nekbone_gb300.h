@@ -191,13 +191,14 @@ void nb_set_mixed_tensor_cores(int on);
  * first form reads and writes x half as often and takes n more floats of
  * scratch. */
 void nb_set_mixed_paired_update(int on);
-/* Mixed solver: 1 (default) checks once per solve whether the FP32 copy of
- * c is, bitwise at every point, a box mesh's inverse multiplicity (2^-m, m
- * the number of the point's extreme local indices on element faces with a
- * neighbour; even lx1 from 4 to 16), and if so the inner CG's fused
- * iteration forms c instead of reading it (4 bytes a point less in the
- * update, the interior's c = 1 not read by the operator); 0 always reads c.
- * The same values either way (bitwise-equal results). */
+/* Mixed solver and batched solve: 1 (default) checks whether the FP32 copy
+ * of c is, bitwise at every point, a box mesh's inverse multiplicity (2^-m,
+ * m the number of the point's extreme local indices on element faces with
+ * a neighbour; even lx1 from 4 to 16) -- once per mixed solve, once per
+ * nb_batch_setup -- and if so the inner CG's fused iteration forms c
+ * instead of reading it (4 bytes a point less in the update, the
+ * interior's c = 1 not read by the operator); 0 always reads c.  The same
+ * values either way (bitwise-equal results). */
 void nb_set_mixed_closed_multiplicity(int on);
 /* The mesh's gather-scatter groups (jl order: groups by primary, members
  * ascending) as CSR: *ng groups, *nmem members; off (ng+1) and idx (nmem)

@@ -166,17 +166,77 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Each element's face bits (cface: bit 0/1 the faces i = 0 / lx1-1 have a
+// neighbour, 2/3 for j, 4/5 for k; read from c at the face points (1,1),
+// 1/2 with a neighbour), and *ok cleared when any point's c differs bitwise
+// from 2^-m, m the number of its extreme local indices on faces with a
+// neighbour: the form k_bupd makes c in.  One block per element at a time.
+__global__ void k_bc_closed_form(const float *__restrict__ c, const int *__restrict__ el_prob,
+                                 const BatchProb *__restrict__ pb, int nelt,
+                                 unsigned char *__restrict__ cface, int *ok) {
+  __shared__ unsigned fb_s;
+  for (int e = blockIdx.x; e < nelt; e += gridDim.x) {
+    const BatchProb &P = pb[el_prob[e]];
+    const int lx = P.lx, L2 = lx * lx, L3 = L2 * lx;
+    const float *ce = c + P.pt0 + long(e - P.el0) * L3;
+    if (threadIdx.x == 0) {
+      const int m = 1, h = lx - 1;
+      const int pt[6] = {0 + lx * m + L2 * m, h + lx * m + L2 * m, m + 0 + L2 * m,
+                         m + lx * h + L2 * m, m + lx * m + 0,  m + lx * m + L2 * h};
+      unsigned fb = 0;
+      for (int f = 0; f < 6; ++f)
+        if (ce[pt[f]] == 0.5f) fb |= 1u << f;
+      fb_s = fb;
+      cface[e] = (unsigned char)fb;
+    }
+    __syncthreads();
+    const unsigned fb = fb_s;
+    bool good = true;
+    for (int l = threadIdx.x; l < L3; l += blockDim.x) {
+      const int i = l % lx, j = (l / lx) % lx, k = l / L2;
+      const unsigned b = (i == 0 ? 1u : 0u) | (i == lx - 1 ? 2u : 0u) | (j == 0 ? 4u : 0u) |
+                         (j == lx - 1 ? 8u : 0u) | (k == 0 ? 16u : 0u) |
+                         (k == lx - 1 ? 32u : 0u);
+      good &= __float_as_uint(ce[l]) == unsigned(127 - __popc(b & fb)) << 23;
+    }
+    // (also keeps the next element's fb_s write behind every read of this one)
+    if (!__syncthreads_and(good) && threadIdx.x == 0) atomicExch(ok, 0);
+  }
+}
+
+// The extreme-index bits of the points of one element of lx1 points a
+// direction, four points (one byte each: bit 0/1 i = 0 / lx1-1, 2/3 for j,
+// 4/5 for k) a word
+std::vector<unsigned> ext_table(int lx) {
+  const int L2 = lx * lx, Q4 = L2 * lx / 4;
+  std::vector<unsigned> t(Q4, 0u);
+  for (int q = 0; q < Q4; ++q)
+    for (int d = 0; d < 4; ++d) {
+      const int l = 4 * q + d, i = l % lx, j = (l / lx) % lx, k = l / L2;
+      const unsigned b = (i == 0 ? 1u : 0u) | (i == lx - 1 ? 2u : 0u) | (j == 0 ? 4u : 0u) |
+                         (j == lx - 1 ? 8u : 0u) | (k == 0 ? 16u : 0u) |
+                         (k == lx - 1 ? 32u : 0u);
+      t[q] |= b << (8 * d);
+    }
+  return t;
+}
+
 // Inner FP32 update (k_cg_update per problem): x += alpha p, r -= alpha w,
 // r'Cr; the problem's last chunk forms rtz1 and beta (z = r), counts the
 // iteration and, with itol > 0, ends the problem's inner CG of this cycle
 // once r'Cr <= itol^2 of the cycle's first (it: the iteration within the
 // cycle, at most max_inner).
+// With cface (c verified as each problem's inverse multiplicity,
+// k_bc_closed_form), the 16-byte path forms c = 2^-m from the element's
+// face bits and the extreme-index bits of the point (ext4: four points a
+// word, one table per lx1 at P.ext0) instead of reading it: the same values.
 __global__ void __launch_bounds__(kThreads)
     k_bupd(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
            const float *__restrict__ w, const float *__restrict__ c,
            const long *__restrict__ pch_q0, const int *__restrict__ pch_prob,
            const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_pt,
-           unsigned *cnt, int it, int max_inner, double itol) {
+           unsigned *cnt, int it, int max_inner, double itol,
+           const unsigned char *__restrict__ cface, const unsigned *__restrict__ ext4) {
   __shared__ double red[32];
   const int ch = blockIdx.x;
   const int prob = pch_prob[ch];
@@ -188,7 +248,47 @@ __global__ void __launch_bounds__(kThreads)
   const uintptr_t al = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
                        reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(w) |
                        reinterpret_cast<uintptr_t>(c);
-  if ((al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
+  if (cface && (al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
+    // the 16-byte path below with c formed: element le of the problem and
+    // group l4 of v, advanced by the stride's quotient and remainder
+    const BatchProb P = pb[prob];
+    const int Q4 = P.lx * P.lx * P.lx / 4;
+    const long vrel = (q0 - P.pt0) / 4 + threadIdx.x;
+    long le = vrel / Q4;
+    int l4 = int(vrel - le * Q4);
+    const int se = kThreads / Q4, sl = kThreads - se * Q4;
+    for (long v = q0 / 4 + threadIdx.x; v < q1 / 4; v += kThreads) {
+      const float4 pv = reinterpret_cast<const float4 *>(p)[v];
+      const float4 wv = reinterpret_cast<const float4 *>(w)[v];
+      float4 rv = reinterpret_cast<const float4 *>(r)[v];
+      float4 xv = reinterpret_cast<const float4 *>(x)[v];
+      const unsigned fb = __ldg(cface + P.el0 + le), b4 = __ldg(ext4 + P.ext0 + l4);
+      float cv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        cv[q] = __int_as_float((127 - __popc((b4 >> (8 * q)) & fb)) << 23);
+      l4 += sl;
+      le += se;
+      if (l4 >= Q4) {
+        l4 -= Q4;
+        ++le;
+      }
+      xv.x = fma_rn(alpha, pv.x, xv.x);
+      xv.y = fma_rn(alpha, pv.y, xv.y);
+      xv.z = fma_rn(alpha, pv.z, xv.z);
+      xv.w = fma_rn(alpha, pv.w, xv.w);
+      rv.x = fma_rn(alphm, wv.x, rv.x);
+      rv.y = fma_rn(alphm, wv.y, rv.y);
+      rv.z = fma_rn(alphm, wv.z, rv.z);
+      rv.w = fma_rn(alphm, wv.w, rv.w);
+      reinterpret_cast<float4 *>(x)[v] = xv;
+      reinterpret_cast<float4 *>(r)[v] = rv;
+      part = fma_rn(mul_rn(rv.x, cv[0]), rv.x, part);
+      part = fma_rn(mul_rn(rv.y, cv[1]), rv.y, part);
+      part = fma_rn(mul_rn(rv.z, cv[2]), rv.z, part);
+      part = fma_rn(mul_rn(rv.w, cv[3]), rv.w, part);
+    }
+  } else if ((al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
     // 16-byte accesses: chunk bounds are multiples of 4 (every lx1^3 of an
     // even lx1 is)
     for (long v = q0 / 4 + threadIdx.x; v < q1 / 4; v += kThreads) {
@@ -517,6 +617,12 @@ struct Batch {
   unsigned *idx = nullptr, *cnt = nullptr;
   long *pch_q0 = nullptr;
   BatchProb *pb = nullptr;
+  // c32 verified (at setup) as every problem's inverse multiplicity: the
+  // elements' face bits, the extreme-index tables of each lx1, one flag
+  unsigned char *cface = nullptr;
+  unsigned *ext4 = nullptr;
+  int *cf_flag = nullptr;
+  bool cf_ok = false;
   BatchScalars *sc = nullptr;
   double *part_ax = nullptr, *part_gs = nullptr, *part_pt = nullptr;
   bool setup_done = false;
@@ -525,7 +631,7 @@ struct Batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   double g_tol = -1.0, g_itol = -1.0;
-  int g_inner = -1, g_outer = -1, g_wtest = -1;
+  int g_inner = -1, g_outer = -1, g_wtest = -1, g_cf = -1;
   double itol = 0.0;  // 0: every cycle runs inner iterations; > 0: per-problem stop
 
   ~Batch() {
@@ -538,11 +644,13 @@ struct Batch {
     }
     void *ptrs[] = {x, f, g, c, r, w, g32, c32, r32, e32, p32, w32, el_prob, off, gch_g0,
                     gch_prob, pch_prob, cycles, idx, cnt, pch_q0, pb, sc, part_ax, part_gs,
-                    part_pt};
+                    part_pt, cface, ext4, cf_flag};
     for (void *p : ptrs)
       if (p) cudaFree(p);
   }
 
+  // c formed in closed form by the inner iteration (verified at setup)
+  bool closed_c() const { return cf_ok && g_mixed_closed_c; }
   int launch_inner_ax(int it, cudaStream_t s) const {
     for (const auto &G : groups) {
       BaxArgs<float> a{};
@@ -551,6 +659,7 @@ struct Batch {
       a.p = p32;
       a.g = g32;
       a.c = c32;
+      a.c_unit_interior = closed_c() ? 1 : 0;
       a.D = G.D32;
       a.eo_h = G.EO.empty() ? nullptr : G.EO.data();
       a.el_prob = el_prob;
@@ -662,7 +771,8 @@ struct Batch {
     NB_CUDA(cudaGetLastError());
     NB_TRY(mark(mk ? mk + 1 : nullptr, s));
     k_bupd<<<npc, kThreads, 0, s>>>(e32, r32, p32, w32, c32, pch_q0, pch_prob, pb, sc, part_pt,
-                                     cnt + nprob, it, max_inner, itol);
+                                     cnt + nprob, it, max_inner, itol,
+                                     closed_c() ? cface : nullptr, ext4);
     NB_CUDA(cudaGetLastError());
     NB_TRY(mark(mk ? mk + 2 : nullptr, s));
     return NB_OK;
@@ -771,7 +881,7 @@ struct Batch {
 
   int build_graph(double tol, int inner, int max_outer) {
     if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer && itol == g_itol &&
-        wait_test_mode() == g_wtest)
+        wait_test_mode() == g_wtest && int(closed_c()) == g_cf)
       return NB_OK;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -840,6 +950,7 @@ struct Batch {
     g_outer = max_outer;
     g_itol = itol;
     g_wtest = wait_test_mode();
+    g_cf = int(closed_c());
     return NB_OK;
   }
 };
@@ -902,10 +1013,10 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
   // concatenation
   B->P.resize(nprob);
   std::vector<int> el_prob, off_all, gch_g0, gch_prob, pch_prob;
-  std::vector<unsigned> idx_all;
+  std::vector<unsigned> idx_all, ext_all;
   std::vector<long> pch_q0;
   long pt = 0;
-  int el = 0, gbase = 0;
+  int el = 0, gbase = 0, ext_lx0 = 0;
   for (int s = 0; s < nprob; ++s) {
     const int p = order[s];
     const long l3 = long(lx[p]) * lx[p] * lx[p];
@@ -917,6 +1028,13 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
     Q.n = nelt * l3;
     Q.el0 = el;
     Q.nelt = int(nelt);
+    Q.lx = lx[p];
+    if (s == 0 || lx[order[s - 1]] != lx[p]) {  // problems are sorted by lx1
+      ext_lx0 = int(ext_all.size());
+      const std::vector<unsigned> t = ext_table(lx[p]);
+      ext_all.insert(ext_all.end(), t.begin(), t.end());
+    }
+    Q.ext0 = ext_lx0;
     for (long e = 0; e < nelt; ++e) el_prob.push_back(s);
     const int ngp = int(offs[s].size()) - 1;
     for (int q = 0; q < ngp; ++q)
@@ -981,6 +1099,9 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
   NB_TRY(upload(&B->pch_q0, pch_q0));
   NB_TRY(upload(&B->pch_prob, pch_prob));
   NB_TRY(upload(&B->pb, B->P));
+  NB_TRY(upload(&B->ext4, ext_all));
+  NB_TRY(dalloc(&B->cface, size_t(B->nelt)));
+  NB_TRY(dalloc(&B->cf_flag, 1));
   NB_TRY(dalloc(&B->sc, nprob));
   NB_TRY(dalloc(&B->cnt, 4 * size_t(nprob)));
   NB_TRY(dalloc(&B->cycles, 1));
@@ -1136,6 +1257,13 @@ int nb_batch_setup(nb_batch *b, uint64_t seed) {
   k_conv<float, double><<<grid_for(6 * B.n), 256, 0, s>>>(B.g32, B.g, 6 * B.n);
   k_conv<float, double><<<grid_for(B.n), 256, 0, s>>>(B.c32, B.c, B.n);
   NB_CUDA(cudaGetLastError());
+  // whether c32 is every problem's inverse multiplicity in closed form
+  NB_CUDA(cudaMemsetAsync(B.cf_flag, 0xFF, sizeof(int), s));
+  k_bc_closed_form<<<std::max(1, std::min(B.nelt, grid_for(long(B.nelt) * 256))), 256, 0, s>>>(
+      B.c32, B.el_prob, B.pb, B.nelt, B.cface, B.cf_flag);
+  NB_CUDA(cudaGetLastError());
+  int cf_h = 0;
+  NB_CUDA(cudaMemcpyAsync(&cf_h, B.cf_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
   // the fixed-point metric (allocated here, outside any graph capture;
   // every solve converts it again)
   for (auto &G : B.groups)
@@ -1144,6 +1272,7 @@ int nb_batch_setup(nb_batch *b, uint64_t seed) {
       NB_TRY(metric_fx_prepare(*G.fx, B.g + 6 * G.pt0, s));
     }
   NB_CUDA(cudaStreamSynchronize(s));
+  B.cf_ok = cf_h != 0;
   B.setup_done = true;
   return NB_OK;
 }

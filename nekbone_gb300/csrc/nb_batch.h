@@ -32,6 +32,8 @@ struct BatchProb {
   int el0, nelt;    // elements (global element index)
   int gc0, ngc;     // boundary-group chunks
   int pc0, npc;     // point chunks
+  int lx;           // points per direction
+  int ext0;         // its lx1's extreme-index table in the batch's ext4
 };
 
 // Launch shape of the batched element operator for one lx1.
@@ -68,6 +70,8 @@ struct BaxArgs {
   int first;           // MODE 1: first inner iteration
   unsigned *err;       // device error word (bounded waits on the metric copy)
   int wait_test;       // timeout self-test of that wait (block_copy_begin)
+  int c_unit_interior;  // MODE 1: c verified as the inverse multiplicity, so 1
+                        //   at element-interior points: not read there
 };
 
 // The batched element operator for one lx1 (T float: MODE 1, T double:

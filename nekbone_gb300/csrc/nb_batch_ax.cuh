@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(LX * LX * EPB)
 #pragma unroll
       for (int k = 1; k < LX - 1; ++k) {
         const size_t id = base + size_t(k) * L2 + tid;
-        creg[k] = a.c[id];
+        creg[k] = (MODE == 1 && a.c_unit_interior) ? T(1) : a.c[id];
         if (MODE == 2) freg[k] = a.f[id];
       }
     }
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(LX * LX)
 #pragma unroll
     for (int k = 1; k < LX - 1; ++k) {
       const size_t id = base + size_t(k) * L2 + t;
-      creg[k] = a.c[id];
+      creg[k] = (MODE == 1 && a.c_unit_interior) ? T(1) : a.c[id];
       if (MODE == 2) freg[k] = a.f[id];
     }
   }

@@ -222,6 +222,9 @@ int launch_cg_update(const Operator &op, CgWork &wk, double *x, double *r,
 int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
                 const double *c, double *r, double *w, double *p, double *z,
                 int it0, int it1, Precond *M, cudaStream_t s);
+// nb_set_mixed_closed_multiplicity: the inner FP32 CGs (single mesh and
+// batched) form c in closed form where it verifies (default true)
+extern bool g_mixed_closed_c;
 // Whether the FP32 c is, bitwise at every point, 2^-m with m the number of
 // the point's extreme local indices whose element face has a neighbour (a
 // box mesh's inverse multiplicity): then *closed and cface[e] holds element

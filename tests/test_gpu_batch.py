@@ -143,6 +143,32 @@ def test_shapes_bit_identical(torch):
     b.close()
 
 
+@pytest.mark.parametrize("itol", [0.0, 1e-4])
+def test_closed_multiplicity_bit_identical(torch, itol):
+    """The inner CG with c formed in closed form (c verified at setup as
+    every problem's inverse multiplicity; the default) and with c read give
+    bit-identical solutions, per-problem results and cycle counts, with a
+    fixed inner count and with per-problem inner stops."""
+    import nekbone_gb300 as nb
+    b = nb.Batch(BOXES)
+    b.setup(23)
+    b.set_inner_tol(itol)
+    got = []
+    try:
+        for closed in (True, False, True):
+            nb.set_mixed_closed_multiplicity(closed)
+            b.solve(1e-10, 20, 40)
+            nb.sync()
+            x = _view(torch, b.arrays()[0], b.n).cpu().numpy().copy()
+            got.append((x, [b.result(p) for p in range(b.nprob)], b.cycles()))
+    finally:
+        nb.set_mixed_closed_multiplicity(True)
+    for x, res, cyc in got[1:]:
+        assert np.array_equal(x, got[0][0])
+        assert res == got[0][1] and cyc == got[0][2]
+    b.close()
+
+
 def test_cycle_bound_and_zero_rhs(torch):
     import nekbone_gb300 as nb
     boxes = [(2, 2, 2, 6), (1, 1, 1, 8), (2, 1, 1, 4)]
