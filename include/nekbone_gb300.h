@@ -183,14 +183,15 @@ void nb_set_shared_metric(int on);
  * products, update); 0 (default) the fused CUDA-core iteration.  The FP64
  * defect correction is the same either way, so both reach the tolerance. */
 void nb_set_mixed_tensor_cores(int on);
-/* Mixed solver: 1 (default) the fused inner FP32 CG keeps its directions in
+/* CG (cg_, nb_cg: the fused FP64 iteration without preconditioner) and the
+ * mixed solver's inner FP32 CG: 1 (default) keeps the search directions in
  * two buffers, odd and even iterations alternating, and updates x once per
- * two iterations (x += a_k p_k, then x += a_k+1 p_k+1, in one pass); 0 one
- * direction buffer and an x update every iteration.  The same fused
- * multiply-adds in the same order either way (bitwise-equal results); the
- * first form reads and writes x half as often and takes n more floats of
- * scratch. */
-void nb_set_mixed_paired_update(int on);
+ * two iterations (x += a_k p_k, then x += a_k+1 p_k+1, in one pass; the
+ * last direction is copied to the caller's p); 0 one direction buffer and
+ * an x update every iteration.  The same fused multiply-adds in the same
+ * order either way (bitwise-equal results); the first form reads and
+ * writes x half as often and takes n more values of device memory. */
+void nb_set_paired_update(int on);
 /* Mixed solver and batched solve: 1 (default) checks whether the FP32 copy
  * of c is, bitwise at every point, a box mesh's inverse multiplicity (2^-m,
  * m the number of the point's extreme local indices on element faces with

@@ -59,7 +59,7 @@ EXPORTS = (
     "nb_batch_rhs_in", "nb_batch_x_out", "nb_set_setup_on_device", "nb_set_mg_fixed_kernels", "nb_set_shared_metric", "nb_mesh_gs_maps",
     "nb_mesh_boundary_groups", "nb_mesh_mask_list", "nekbone_cg_report_",
     "nb_mg_setup_coarse", "nb_eo_line_maps", "nb_set_mixed_tensor_cores",
-    "nb_set_mixed_paired_update", "nb_set_mixed_closed_multiplicity",
+    "nb_set_paired_update", "nb_set_mixed_closed_multiplicity",
     "nb_wait_selftest", "nb_set_wait_test", "nb_pipe_rates",
 )
 
@@ -133,8 +133,8 @@ lib.nb_set_shared_metric.restype = None
 lib.nb_set_shared_metric.argtypes = [_i]
 lib.nb_set_mixed_tensor_cores.restype = None
 lib.nb_set_mixed_tensor_cores.argtypes = [_i]
-lib.nb_set_mixed_paired_update.restype = None
-lib.nb_set_mixed_paired_update.argtypes = [_i]
+lib.nb_set_paired_update.restype = None
+lib.nb_set_paired_update.argtypes = [_i]
 lib.nb_set_mixed_closed_multiplicity.restype = None
 lib.nb_set_mixed_closed_multiplicity.argtypes = [_i]
 lib.nb_wait_selftest.restype = _i
@@ -678,11 +678,11 @@ def set_mixed_tensor_cores(on: bool) -> None:
     lib.nb_set_mixed_tensor_cores(1 if on else 0)
 
 
-def set_mixed_paired_update(on: bool) -> None:
-    """Mixed solver: the inner FP32 CG's x updated once per two iterations
-    from two direction buffers (True, default) or every iteration (False);
-    bitwise the same iterates."""
-    lib.nb_set_mixed_paired_update(1 if on else 0)
+def set_paired_update(on: bool) -> None:
+    """FP64 CG (fused, no preconditioner) and the mixed solver's inner FP32
+    CG: x updated once per two iterations from two direction buffers (True,
+    default) or every iteration (False); bitwise the same iterates."""
+    lib.nb_set_paired_update(1 if on else 0)
 
 
 def set_mixed_closed_multiplicity(on: bool) -> None:

@@ -325,7 +325,7 @@ __device__ __forceinline__ void ax_fx_body(const AxArgs<double> &a, const FxCoef
       const size_t id = base + size_t(k) * L2 + t;
       if (MODE == 1) {
         uk[k] = a.u[id];
-        pold[k] = a.first ? 0.0 : a.p[id];
+        pold[k] = a.first ? 0.0 : a.pold[id];
       } else if (MODE == 2) {
         uk[k] = a.p[id];
         pold[k] = a.e ? double(a.e[id]) : 0.0;

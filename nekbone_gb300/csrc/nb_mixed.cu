@@ -208,9 +208,9 @@ void set_shared_metric(bool on) { g_shared_metric = on; }
 // the inner CG's element products on the tensor cores (k_ax_tc: FP16 hi+lo
 // split operands, FP32 accumulation) instead of the fused CUDA-core pass
 bool g_mixed_tc = false;
-// the inner CG's x updated once per two iterations from two direction
-// buffers (cg_device_f32's p_alt; bitwise the same iterates)
-bool g_mixed_paired = true;
+// x updated once per two iterations from two direction buffers (the FP64
+// CG's and the inner CG's p_alt; bitwise the same iterates)
+bool g_paired_update = true;
 // the inner CG forms c in closed form where c verifies as a box mesh's
 // inverse multiplicity (c_closed_form; the same values)
 bool g_mixed_closed_c = true;
@@ -241,7 +241,7 @@ extern "C" {
 
 void nb_set_shared_metric(int on) { set_shared_metric(on != 0); }
 void nb_set_mixed_tensor_cores(int on) { g_mixed_tc = on != 0; }
-void nb_set_mixed_paired_update(int on) { g_mixed_paired = on != 0; }
+void nb_set_paired_update(int on) { g_paired_update = on != 0; }
 void nb_set_mixed_closed_multiplicity(int on) { g_mixed_closed_c = on != 0; }
 
 int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
@@ -302,7 +302,7 @@ int nb_cg_mixed(nb_mesh *mesh, double *x, const double *f, const double *g,
     wk.c32_face = closed ? cface : nullptr;
     if (!st)
       st = cg_device_f32(op, wk, e32, r32, g32, c32, rr32, w32, p32, inner_iters, s,
-                         g_mixed_paired ? p32b : nullptr);
+                         g_paired_update ? p32b : nullptr);
     wk.g32_uniform = 0;
     wk.tc_inner = false;
     wk.c32_face = nullptr;

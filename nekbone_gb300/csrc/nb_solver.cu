@@ -39,6 +39,18 @@ CgWork::~CgWork() {
   if (counters) cudaFree(counters);
   if (sc) cudaFree(sc);
   if (scratch) cudaFree(scratch);
+  if (palt) cudaFree(palt);
+}
+
+int CgWork::ensure_palt(long n) {
+  if (palt && palt_n >= n) return NB_OK;
+  if (palt) cudaFree(palt);
+  palt = nullptr;
+  palt_n = 0;
+  if (cudaMalloc(&palt, size_t(n) * sizeof(double)) != cudaSuccess)
+    return fail(NB_ERR_CUDA, "CG direction buffer: out of device memory (%ld points)", n);
+  palt_n = n;
+  return NB_OK;
 }
 
 int CgWork::ensure_scratch(size_t bytes) {
@@ -657,10 +669,11 @@ static int cg_begin_t(Operator &op, CgWork &wk, T *x, const T *f, const T *c,
   return vec_glsc3<T>(r, c, r, n, wk, wk.dot_out, wk.sc, 1, 0, s);
 }
 
-// iterations it0..it1 of cg.f:48-75.  With p_alt (the fused FP32 inner CG
-// from its first iteration), the directions of odd iterations go to p and
-// those of even iterations to p_alt, and each pair of iterations updates x
-// once (k_cg_update DEFER 1, then 2).
+// iterations it0..it1 of cg.f:48-75.  With p_alt (the fused, unpreconditioned
+// iteration), the directions of odd iterations go to p and those of even
+// iterations to p_alt, and each pair (odd, even) of iterations inside
+// it0..it1 updates x once (k_cg_update DEFER 1, then 2); the direction of
+// an even last iteration stays in p_alt (cg_device copies it to p).
 template <typename T>
 static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
                       T *r, T *w, T *p, T *z, int it0, int it1, int niter,
@@ -670,7 +683,7 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
   const T *D = std::is_same<T, double>::value ? (const T *)op.dD : (const T *)op.fD;
   const bool tc = std::is_same<T, float>::value && wk.tc_inner;
   const bool fused = op.fused_ok && !force_unfused && !tc;
-  const bool paired = p_alt && fused && !M && it0 == 1;
+  const bool paired = p_alt && fused && !M;
   T *const p_odd = p;
   for (int iter = it0; iter <= it1; ++iter) {
     T *pold = nullptr;
@@ -735,7 +748,7 @@ static int cg_steps_t(Operator &op, CgWork &wk, T *x, const T *g, const T *c,
     double *hist = iter < wk.hist_len ? wk.hist : nullptr;
     if (paired && (iter & 1) && iter < it1)
       update_launch<T, 1>(op, wk, x, r, p, w, c, hist, iter, 1, nullptr, nullptr, s);
-    else if (paired && !(iter & 1))
+    else if (paired && !(iter & 1) && iter > it0)
       update_launch<T, 2>(op, wk, x, r, p, w, c, hist, iter, 1, nullptr, pold, s);
     else
       update_launch<T, 0>(op, wk, x, r, p, w, c, hist, iter, M == nullptr, r32, nullptr, s);
@@ -877,8 +890,19 @@ int cg_device(Operator &op, CgWork &wk, double *x, const double *f,
               double *p, double *z, int niter, Precond *M, bool force_unfused,
               cudaStream_t s) {
   NB_TRY(cg_begin_t<double>(op, wk, x, f, c, r, true, niter, s));
-  return cg_steps_t<double>(op, wk, x, g, c, r, w, p, z, 1, niter, niter, M,
-                            force_unfused, s);
+  // the second direction buffer of the paired x update (fused, no
+  // preconditioner, at least one pair)
+  double *p_alt = nullptr;
+  if (g_paired_update && !M && !force_unfused && op.fused_ok && niter >= 2) {
+    NB_TRY(wk.ensure_palt(op.n));
+    p_alt = wk.palt;
+  }
+  NB_TRY(cg_steps_t<double>(op, wk, x, g, c, r, w, p, z, 1, niter, niter, M,
+                            force_unfused, s, p_alt));
+  // the last direction is the caller's p (cg.f's p on return)
+  if (p_alt && niter % 2 == 0)
+    NB_CUDA(cudaMemcpyAsync(p, p_alt, op.n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return NB_OK;
 }
 
 int cg_begin(Operator &op, CgWork &wk, double *x, const double *f,

@@ -89,9 +89,13 @@ struct CgWork {
   // multiplicity (c_closed_form): each element's face bits; the fused
   // iteration then forms c instead of reading it (same values)
   const unsigned char *c32_face = nullptr;
+  // the FP64 CG's second direction buffer (paired x update)
+  double *palt = nullptr;
+  long palt_n = 0;
   ~CgWork();
   int ensure(const Operator &op, int niter);
   int ensure_scratch(size_t bytes);
+  int ensure_palt(long n);
 };
 
 // Builds the operator for a box of nelx*nely*nelz elements with lx points
@@ -225,6 +229,10 @@ int cg_steps_pc(Operator &op, CgWork &wk, double *x, const double *g,
 // nb_set_mixed_closed_multiplicity: the inner FP32 CGs (single mesh and
 // batched) form c in closed form where it verifies (default true)
 extern bool g_mixed_closed_c;
+// nb_set_paired_update: the fused FP64 CG (cg_device) and the mixed
+// solver's inner CG alternate two direction buffers and update x once per
+// pair of iterations (default true)
+extern bool g_paired_update;
 // Whether the FP32 c is, bitwise at every point, 2^-m with m the number of
 // the point's extreme local indices whose element face has a neighbour (a
 // box mesh's inverse multiplicity): then *closed and cface[e] holds element

@@ -407,7 +407,7 @@ def test_mixed_inner_forms_bitwise(nb, lx, inner, mask):
     xs = {}
     try:
         for paired, closed in ((True, True), (False, True), (True, False), (False, False)):
-            nb.set_mixed_paired_update(paired)
+            nb.set_paired_update(paired)
             nb.set_mixed_closed_multiplicity(closed)
             x = torch.zeros(n, dtype=torch.float64, device=dev)
             outer, tot, rr = m.cg_mixed(x.data_ptr(), f.data_ptr(), g.data_ptr(),
@@ -415,12 +415,48 @@ def test_mixed_inner_forms_bitwise(nb, lx, inner, mask):
             assert rr <= 1e-10 or not mask
             xs[paired, closed] = (x.cpu().numpy(), outer, rr)
     finally:
-        nb.set_mixed_paired_update(True)
+        nb.set_paired_update(True)
         nb.set_mixed_closed_multiplicity(True)
     ref = xs[False, False]
     for key, got in xs.items():
         assert got[1:] == ref[1:], key
         assert np.array_equal(got[0], ref[0]), key
+
+
+@pytest.mark.parametrize("niter", [9, 10])
+@pytest.mark.parametrize("order", [2, 1])
+def test_cg_paired_update_bitwise(nb, niter, order):
+    """The FP64 CG with two direction buffers and one x update per pair of
+    iterations gives bitwise the x, r, w, p, z and residual history of one
+    buffer and an update every iteration, with the fixed-point (order 2) and
+    the even-odd FP64 (order 1) operator; an even count ends with the last
+    direction in the second buffer, copied to p."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(4, 3, 5, 8, mask_mode=1)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g_deformed(g.data_ptr(), 7, 0.1)
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 19)
+    outs = {}
+    try:
+        m.set_order(order)
+        for paired in (True, False):
+            nb.set_paired_update(paired)
+            x, r, w, p, z = (torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+                             for _ in range(5))
+            h = m.cg(*(t.data_ptr() for t in (x, f, g, c, r, w, p, z)), niter, hist=True)
+            torch.cuda.synchronize()
+            outs[paired] = ([t.cpu().numpy() for t in (x, r, w, p, z)], h)
+    finally:
+        nb.set_paired_update(True)
+        m.set_order(nb.DEFAULT_ORDER)
+    for name, a, b in zip("xrwpz", outs[True][0], outs[False][0]):
+        assert np.array_equal(a, b), name
+    assert np.array_equal(outs[True][1], outs[False][1])
 
 
 def test_mixed_closed_multiplicity_rejects_other_c(nb):
