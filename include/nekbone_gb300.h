@@ -357,14 +357,16 @@ int nb_sync(void);
 void *nb_stream(void);
 /* Average device time (ms) of each kernel of one fused FP64 CG iteration --
  * [0] element operator + direction update, [1] boundary gather-scatter and
- * pap, [2] x/r update and rtr -- over reps iterations, timed with CUDA
- * events on the library stream.  Vectors as for nb_cg; x and r are
- * overwritten. */
+ * pap, [2] x/r update and rtr -- over reps iterations (over 2 reps with
+ * the paired x update of nb_set_paired_update, its two update forms
+ * averaged), timed with CUDA events on the library stream.  Vectors as for nb_cg; x
+ * and r are overwritten. */
 int nb_time_cg_kernels(nb_mesh *mesh, double *x, const double *f,
                        const double *g, const double *c, double *r, double *w,
                        double *p, int reps, double *ms3);
 /* The same for the FP32 iteration of the mixed solver's inner CG (float
- * device vectors, g as 6n floats). */
+ * device vectors, g as 6n floats; c formed in closed form when it verifies,
+ * as the inner CG does). */
 int nb_time_cg_kernels_f32(nb_mesh *mesh, float *x, const float *f,
                            const float *g, const float *c, float *r, float *w,
                            float *p, int reps, double *ms3);

@@ -787,17 +787,17 @@ template <typename T>
 int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
                       const T *c, T *r, T *w, T *p, int reps, double *ms3,
                       cudaStream_t s) {
-  // FP32: the mixed solver's inner CG form, directions alternating between
-  // p and a second buffer, x updated once per pair of iterations, and c
-  // formed in closed form where it verifies
-  constexpr bool PAIRED = std::is_same<T, float>::value;
+  // the solvers' forms: directions alternating between p and a second
+  // buffer, x updated once per pair of iterations (nb_set_paired_update),
+  // and for FP32 c formed in closed form where it verifies
+  // (nb_set_mixed_closed_multiplicity)
+  const bool PAIRED = g_paired_update;
+  constexpr bool F32 = std::is_same<T, float>::value;
   const int iters = PAIRED ? 2 * reps : reps;
   T *p_alt = nullptr;
   unsigned char *cface = nullptr;
-  if (PAIRED) {
-    NB_CUDA(cudaMalloc(&p_alt, op.n * sizeof(T)));
-    NB_CUDA(cudaMalloc(&cface, size_t(op.nelt) + 16));
-  }
+  if (PAIRED) NB_CUDA(cudaMalloc(&p_alt, op.n * sizeof(T)));
+  if (F32 && g_mixed_closed_c) NB_CUDA(cudaMalloc(&cface, size_t(op.nelt) + 16));
   std::unique_ptr<T, int (*)(T *)> p_alt_owner(p_alt, [](T *q) { return int(cudaFree(q)); });
   std::unique_ptr<unsigned char, int (*)(unsigned char *)> cface_owner(
       cface, [](unsigned char *q) { return int(cudaFree(q)); });
@@ -805,11 +805,13 @@ int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
     CgWork &wk;
     ~FaceReset() { wk.c32_face = nullptr; }
   } face_reset{wk};
-  if constexpr (PAIRED) {
-    bool closed = false;
-    int *flag = reinterpret_cast<int *>(cface + ((size_t(op.nelt) + 3) & ~size_t(3)));
-    NB_TRY(c_closed_form(op, (const float *)c, cface, flag, &closed, s));
-    wk.c32_face = closed ? cface : nullptr;
+  if constexpr (F32) {
+    if (cface) {
+      bool closed = false;
+      int *flag = reinterpret_cast<int *>(cface + ((size_t(op.nelt) + 3) & ~size_t(3)));
+      NB_TRY(c_closed_form(op, (const float *)c, cface, flag, &closed, s));
+      wk.c32_face = closed ? cface : nullptr;
+    }
   }
   NB_TRY(cg_begin_t<T>(op, wk, x, f, c, r, true, iters + 2, s));
   NB_TRY(cg_steps_t<T>(op, wk, x, g, c, r, w, p, r, 1, 1, -1, nullptr, false, s));

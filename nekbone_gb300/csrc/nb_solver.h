@@ -210,8 +210,10 @@ int cg_steps(Operator &op, CgWork &wk, double *x, const double *g,
 int residual_fused(Operator &op, CgWork &wk, double *x, const float *e,
                    double scale, const double *f, const double *g,
                    const double *c, double *r, double *w, cudaStream_t s);
-// CUDA-event times of the three kernels of a fused CG iteration (FP32: the
-// average over a pair of iterations with the paired x update)
+// CUDA-event times of the three kernels of a fused CG iteration, in the
+// solvers' form: with the paired x update (nb_set_paired_update) the
+// average over pairs of iterations; FP32 with c in closed form where it
+// verifies (nb_set_mixed_closed_multiplicity)
 template <typename T>
 int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
                       const T *c, T *r, T *w, T *p, int reps, double *ms3,
