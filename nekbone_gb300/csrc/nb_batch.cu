@@ -696,6 +696,7 @@ struct Batch {
       a.el_prob = el_prob + G.el0;
       a.act = &sc[0].active;
       a.act_stride = int(sizeof(BatchScalars) / sizeof(int));
+      a.err = device_error_word();
       return launch_ax_fx_m2(*G.fx, a, s);
     }
     BaxArgs<double> a{};

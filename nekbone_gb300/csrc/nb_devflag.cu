@@ -24,8 +24,9 @@ unsigned *device_error_word() {
   return g_err;
 }
 
-// Fails with NB_ERR_CUDA when a kernel reported a wait that ran out (and
-// clears the word).  Synchronises the stream.
+// Fails with NB_ERR_CUDA when a kernel reported a wait that ran out (bit 0)
+// or a fixed-point range check that failed (bit 1), and clears the word.
+// Synchronises the stream.
 int device_error_check(cudaStream_t s) {
   NB_CUDA(cudaStreamSynchronize(s));
   if (!g_err) return NB_OK;
@@ -33,7 +34,10 @@ int device_error_check(cudaStream_t s) {
   NB_CUDA(cudaMemcpy(&v, g_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
   if (v) {
     cudaMemset(g_err, 0, sizeof(unsigned));
-    return fail(NB_ERR_CUDA, "a device-side wait timed out (flags %u); results are invalid", v);
+    return fail(NB_ERR_CUDA, "%s (flags %u); results are invalid",
+                (v & 1u) ? "a device-side wait timed out"
+                         : "a fixed-point operator's range check failed",
+                v);
   }
   return NB_OK;
 }
