@@ -144,8 +144,11 @@ __device__ __forceinline__ int bexp(double x) {
 }
 
 // x * 2^(1075 - emax + up) rounded to nearest (ties away from zero), for x
-// whose biased exponent is <= emax: |result| < 2^(53 + up)
-__device__ __forceinline__ i64 to_fixed(double x, int emax, int up) {
+// whose biased exponent is <= emax: |result| < 2^(53 + up).  This and
+// to_double are the conversions' fallbacks for exponents out of the fast
+// forms' range; out of line, they leave the operator's code smaller (100 CG
+// iterations at 32^3: 247.0 instead of 248.3 ms).
+static __device__ __noinline__ i64 to_fixed(double x, int emax, int up) {
   const u64 b = u64(__double_as_longlong(x));
   const int e = int((b >> 52) & 0x7FFu);
   const u64 m = (b & 0xFFFFFFFFFFFFFull) | (e ? (1ull << 52) : 0ull);
@@ -158,7 +161,7 @@ __device__ __forceinline__ i64 to_fixed(double x, int emax, int up) {
 }
 
 // W * 2^s rounded to the nearest FP64 value (ties to even)
-__device__ __forceinline__ double to_double(i64 W, int s) {
+static __device__ __noinline__ double to_double(i64 W, int s) {
   if (W == 0) return 0.0;
   const u64 sign = u64(W) & (1ull << 63);
   u64 mag = W < 0 ? u64(-W) : u64(W);
