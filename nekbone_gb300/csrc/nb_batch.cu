@@ -227,85 +227,92 @@ std::vector<unsigned> ext_table(int lx) {
 // once r'Cr <= itol^2 of the cycle's first (it: the iteration within the
 // cycle, at most max_inner).
 // With cface (c verified as each problem's inverse multiplicity,
-// k_bc_closed_form), the 16-byte path forms c = 2^-m from the element's
+// k_bc_closed_form), the 16-byte paths form c = 2^-m from the element's
 // face bits and the extreme-index bits of the point (ext4: four points a
 // word, one table per lx1 at P.ext0) instead of reading it: the same values.
+// DEFER pairs the x updates of two iterations whose directions sit in two
+// buffers (as k_cg_update): 1 leaves x alone, keeps alpha in alpha_prev
+// and marks the problem pending if its inner CG stops here (k_bflush then
+// makes the update); 2 makes x += alpha_prev pprev, x += alpha p, the
+// unpaired form's two fused multiply-adds in order.
+template <int DEFER>
 __global__ void __launch_bounds__(kThreads)
     k_bupd(float *__restrict__ x, float *__restrict__ r, const float *__restrict__ p,
            const float *__restrict__ w, const float *__restrict__ c,
            const long *__restrict__ pch_q0, const int *__restrict__ pch_prob,
            const BatchProb *__restrict__ pb, BatchScalars *sc, double *__restrict__ part_pt,
            unsigned *cnt, int it, int max_inner, double itol,
-           const unsigned char *__restrict__ cface, const unsigned *__restrict__ ext4) {
+           const unsigned char *__restrict__ cface, const unsigned *__restrict__ ext4,
+           const float *__restrict__ pprev) {
   __shared__ double red[32];
   const int ch = blockIdx.x;
   const int prob = pch_prob[ch];
   if (!sc[prob].active || !sc[prob].iactive) return;
   const float alpha = float(sc[prob].alpha);
   const float alphm = -alpha;
+  const float alpha0 = DEFER == 2 ? float(sc[prob].alpha_prev) : 0.f;
   const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
   float part = 0.f;
   const uintptr_t al = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(r) |
                        reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(w) |
-                       reinterpret_cast<uintptr_t>(c);
-  if (cface && (al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
-    // the 16-byte path below with c formed: element le of the problem and
-    // group l4 of v, advanced by the stride's quotient and remainder
+                       reinterpret_cast<uintptr_t>(c) |
+                       (DEFER == 2 ? reinterpret_cast<uintptr_t>(pprev) : uintptr_t(0));
+  if ((al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
+    // 16-byte accesses: chunk bounds are multiples of 4 (every lx1^3 of an
+    // even lx1 is).  With cface: element le of the problem and group l4 of
+    // v, advanced by the stride's quotient and remainder.
     const BatchProb P = pb[prob];
     const int Q4 = P.lx * P.lx * P.lx / 4;
-    const long vrel = (q0 - P.pt0) / 4 + threadIdx.x;
-    long le = vrel / Q4;
-    int l4 = int(vrel - le * Q4);
-    const int se = kThreads / Q4, sl = kThreads - se * Q4;
-    for (long v = q0 / 4 + threadIdx.x; v < q1 / 4; v += kThreads) {
-      const float4 pv = reinterpret_cast<const float4 *>(p)[v];
-      const float4 wv = reinterpret_cast<const float4 *>(w)[v];
-      float4 rv = reinterpret_cast<const float4 *>(r)[v];
-      float4 xv = reinterpret_cast<const float4 *>(x)[v];
-      const unsigned fb = __ldg(cface + P.el0 + le), b4 = __ldg(ext4 + P.ext0 + l4);
-      float cv[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        cv[q] = __int_as_float((127 - __popc((b4 >> (8 * q)) & fb)) << 23);
-      l4 += sl;
-      le += se;
-      if (l4 >= Q4) {
-        l4 -= Q4;
-        ++le;
-      }
-      xv.x = fma_rn(alpha, pv.x, xv.x);
-      xv.y = fma_rn(alpha, pv.y, xv.y);
-      xv.z = fma_rn(alpha, pv.z, xv.z);
-      xv.w = fma_rn(alpha, pv.w, xv.w);
-      rv.x = fma_rn(alphm, wv.x, rv.x);
-      rv.y = fma_rn(alphm, wv.y, rv.y);
-      rv.z = fma_rn(alphm, wv.z, rv.z);
-      rv.w = fma_rn(alphm, wv.w, rv.w);
-      reinterpret_cast<float4 *>(x)[v] = xv;
-      reinterpret_cast<float4 *>(r)[v] = rv;
-      part = fma_rn(mul_rn(rv.x, cv[0]), rv.x, part);
-      part = fma_rn(mul_rn(rv.y, cv[1]), rv.y, part);
-      part = fma_rn(mul_rn(rv.z, cv[2]), rv.z, part);
-      part = fma_rn(mul_rn(rv.w, cv[3]), rv.w, part);
+    long le = 0;
+    int l4 = 0, se = 0, sl = 0;
+    if (cface) {
+      const long vrel = (q0 - P.pt0) / 4 + threadIdx.x;
+      le = vrel / Q4;
+      l4 = int(vrel - le * Q4);
+      se = kThreads / Q4;
+      sl = kThreads - se * Q4;
     }
-  } else if ((al & 15u) == 0 && ((q0 | q1) & 3) == 0) {
-    // 16-byte accesses: chunk bounds are multiples of 4 (every lx1^3 of an
-    // even lx1 is)
     for (long v = q0 / 4 + threadIdx.x; v < q1 / 4; v += kThreads) {
-      const float4 pv = reinterpret_cast<const float4 *>(p)[v];
+      float4 xv = make_float4(0.f, 0.f, 0.f, 0.f), pv = xv, qv = xv, cv = xv;
+      if (DEFER != 1) {
+        pv = reinterpret_cast<const float4 *>(p)[v];
+        xv = reinterpret_cast<const float4 *>(x)[v];
+      }
+      if (DEFER == 2) qv = reinterpret_cast<const float4 *>(pprev)[v];
       const float4 wv = reinterpret_cast<const float4 *>(w)[v];
       float4 rv = reinterpret_cast<const float4 *>(r)[v];
-      float4 xv = reinterpret_cast<const float4 *>(x)[v];
-      const float4 cv = reinterpret_cast<const float4 *>(c)[v];
-      xv.x = fma_rn(alpha, pv.x, xv.x);
-      xv.y = fma_rn(alpha, pv.y, xv.y);
-      xv.z = fma_rn(alpha, pv.z, xv.z);
-      xv.w = fma_rn(alpha, pv.w, xv.w);
+      if (cface) {
+        const unsigned fb = __ldg(cface + P.el0 + le), b4 = __ldg(ext4 + P.ext0 + l4);
+        cv.x = __int_as_float((127 - __popc(b4 & fb)) << 23);
+        cv.y = __int_as_float((127 - __popc((b4 >> 8) & fb)) << 23);
+        cv.z = __int_as_float((127 - __popc((b4 >> 16) & fb)) << 23);
+        cv.w = __int_as_float((127 - __popc((b4 >> 24) & fb)) << 23);
+        l4 += sl;
+        le += se;
+        if (l4 >= Q4) {
+          l4 -= Q4;
+          ++le;
+        }
+      } else {
+        cv = reinterpret_cast<const float4 *>(c)[v];
+      }
+      if (DEFER == 2) {
+        xv.x = fma_rn(alpha0, qv.x, xv.x);
+        xv.y = fma_rn(alpha0, qv.y, xv.y);
+        xv.z = fma_rn(alpha0, qv.z, xv.z);
+        xv.w = fma_rn(alpha0, qv.w, xv.w);
+      }
+      if (DEFER != 1) {
+        xv.x = fma_rn(alpha, pv.x, xv.x);
+        xv.y = fma_rn(alpha, pv.y, xv.y);
+        xv.z = fma_rn(alpha, pv.z, xv.z);
+        xv.w = fma_rn(alpha, pv.w, xv.w);
+      }
       rv.x = fma_rn(alphm, wv.x, rv.x);
       rv.y = fma_rn(alphm, wv.y, rv.y);
       rv.z = fma_rn(alphm, wv.z, rv.z);
       rv.w = fma_rn(alphm, wv.w, rv.w);
-      reinterpret_cast<float4 *>(x)[v] = xv;
+      if (DEFER != 1) reinterpret_cast<float4 *>(x)[v] = xv;
       reinterpret_cast<float4 *>(r)[v] = rv;
       part = fma_rn(mul_rn(rv.x, cv.x), rv.x, part);
       part = fma_rn(mul_rn(rv.y, cv.y), rv.y, part);
@@ -315,8 +322,9 @@ __global__ void __launch_bounds__(kThreads)
   } else {
 #pragma unroll 4
     for (long q = q0 + threadIdx.x; q < q1; q += kThreads) {
-      const float pv = p[q], wv = w[q], rv0 = r[q], xv = x[q], cv = c[q];
-      x[q] = fma_rn(alpha, pv, xv);
+      const float wv = w[q], rv0 = r[q], cv = c[q];
+      if (DEFER == 2) x[q] = fma_rn(alpha, p[q], fma_rn(alpha0, pprev[q], x[q]));
+      else if (DEFER == 0) x[q] = fma_rn(alpha, p[q], x[q]);
       const float rv = fma_rn(alphm, wv, rv0);
       r[q] = rv;
       part = fma_rn(mul_rn(rv, cv), rv, part);
@@ -334,9 +342,29 @@ __global__ void __launch_bounds__(kThreads)
       S.rtz1 = rtr;
       S.beta = S.rtz2 != 0.0 ? S.rtz1 / S.rtz2 : 0.0;
       S.inner += 1;
-      if (it >= max_inner || (itol > 0.0 && rtr <= itol * itol * S.irtr0)) S.iactive = 0;
+      const bool stop = it >= max_inner || (itol > 0.0 && rtr <= itol * itol * S.irtr0);
+      if (stop) S.iactive = 0;
+      if (DEFER == 1) {
+        S.alpha_prev = S.alpha;
+        S.pend = stop ? 1 : 0;
+      }
     }
   }
+}
+
+// The deferred x update of every problem whose inner CG stopped on the
+// first iteration of a pair (pend): x += alpha_prev p, p the direction
+// buffer of odd iterations.  Before the defect, which reads x.
+__global__ void __launch_bounds__(kThreads)
+    k_bflush(float *__restrict__ x, const float *__restrict__ p,
+             const long *__restrict__ pch_q0, const int *__restrict__ pch_prob,
+             const BatchScalars *__restrict__ sc) {
+  const int ch = blockIdx.x;
+  const int prob = pch_prob[ch];
+  if (!sc[prob].active || !sc[prob].pend) return;
+  const float alpha = float(sc[prob].alpha_prev);
+  const long q0 = pch_q0[ch], q1 = pch_q0[ch + 1];
+  for (long q = q0 + threadIdx.x; q < q1; q += kThreads) x[q] = fma_rn(alpha, p[q], x[q]);
 }
 
 // Start of a cycle: inner right-hand side r32 = r / |r|, inner x = 0, and
@@ -370,6 +398,7 @@ __global__ void __launch_bounds__(kThreads)
       sc[prob].irtr0 = rtz;
       sc[prob].beta = 0.0;
       sc[prob].iactive = 1;
+      sc[prob].pend = 0;
     }
   }
 }
@@ -612,6 +641,7 @@ struct Batch {
   double *x = nullptr, *f = nullptr, *g = nullptr, *c = nullptr, *r = nullptr, *w = nullptr;
   float *g32 = nullptr, *c32 = nullptr, *r32 = nullptr, *e32 = nullptr, *p32 = nullptr,
         *w32 = nullptr;
+  float *p32b = nullptr;  // the inner CG's direction buffer of even iterations
   int *el_prob = nullptr, *off = nullptr, *gch_g0 = nullptr, *gch_prob = nullptr,
       *pch_prob = nullptr, *cycles = nullptr;
   unsigned *idx = nullptr, *cnt = nullptr;
@@ -631,7 +661,7 @@ struct Batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   double g_tol = -1.0, g_itol = -1.0;
-  int g_inner = -1, g_outer = -1, g_wtest = -1, g_cf = -1;
+  int g_inner = -1, g_outer = -1, g_wtest = -1, g_cf = -1, g_pair = -1;
   double itol = 0.0;  // 0: every cycle runs inner iterations; > 0: per-problem stop
 
   ~Batch() {
@@ -644,19 +674,25 @@ struct Batch {
     }
     void *ptrs[] = {x, f, g, c, r, w, g32, c32, r32, e32, p32, w32, el_prob, off, gch_g0,
                     gch_prob, pch_prob, cycles, idx, cnt, pch_q0, pb, sc, part_ax, part_gs,
-                    part_pt, cface, ext4, cf_flag};
+                    part_pt, cface, ext4, cf_flag, p32b};
     for (void *p : ptrs)
       if (p) cudaFree(p);
   }
 
   // c formed in closed form by the inner iteration (verified at setup)
   bool closed_c() const { return cf_ok && g_mixed_closed_c; }
+  // the inner CG's directions alternate between p32 (odd iterations) and
+  // p32b (even), and x is updated once per pair (nb_set_paired_update)
+  bool paired() const { return g_paired_update && p32b; }
+  float *dir(int it) const { return paired() && !(it & 1) ? p32b : p32; }
+  float *dir_old(int it) const { return paired() && (it & 1) ? p32b : p32; }
   int launch_inner_ax(int it, cudaStream_t s) const {
     for (const auto &G : groups) {
       BaxArgs<float> a{};
       a.w = w32;
       a.u = r32;
-      a.p = p32;
+      a.p = dir(it);
+      a.pold = dir_old(it);
       a.g = g32;
       a.c = c32;
       a.c_unit_interior = closed_c() ? 1 : 0;
@@ -732,7 +768,8 @@ struct Batch {
     for (const auto &G : groups) NB_TRY(defect_group_ax(G, G.tune.epb64, s));
     return NB_OK;
   }
-  static int batch_ax_f32(int lx, int epb, int rd, const BaxArgs<float> &a, cudaStream_t s) {
+  static int batch_ax_f32(int lx, int epb, int rd, BaxArgs<float> a, cudaStream_t s) {
+    if (!a.pold) a.pold = a.p;  // MODE 1 reads the old direction from pold
     switch (lx) {
       case 4: return batch_ax_f32_lx<4>(epb, rd, a, s);
       case 6: return batch_ax_f32_lx<6>(epb, rd, a, s);
@@ -767,18 +804,33 @@ struct Batch {
                       const cudaEvent_t *mk = nullptr) const {
     NB_TRY(launch_inner_ax(it, s));
     NB_TRY(mark(mk, s));
-    k_bgs_fin<<<ngc, kThreads, 0, s>>>(w32, p32, c32, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
+    float *pc = dir(it);
+    k_bgs_fin<<<ngc, kThreads, 0, s>>>(w32, pc, c32, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
                                        part_ax, cnt);
     NB_CUDA(cudaGetLastError());
     NB_TRY(mark(mk ? mk + 1 : nullptr, s));
-    k_bupd<<<npc, kThreads, 0, s>>>(e32, r32, p32, w32, c32, pch_q0, pch_prob, pb, sc, part_pt,
-                                     cnt + nprob, it, max_inner, itol,
-                                     closed_c() ? cface : nullptr, ext4);
+    const unsigned char *cf = closed_c() ? cface : nullptr;
+    if (paired() && (it & 1) && it < max_inner)
+      k_bupd<1><<<npc, kThreads, 0, s>>>(e32, r32, pc, w32, c32, pch_q0, pch_prob, pb, sc,
+                                         part_pt, cnt + nprob, it, max_inner, itol, cf, ext4,
+                                         nullptr);
+    else if (paired() && !(it & 1))
+      k_bupd<2><<<npc, kThreads, 0, s>>>(e32, r32, pc, w32, c32, pch_q0, pch_prob, pb, sc,
+                                         part_pt, cnt + nprob, it, max_inner, itol, cf, ext4,
+                                         dir_old(it));
+    else
+      k_bupd<0><<<npc, kThreads, 0, s>>>(e32, r32, pc, w32, c32, pch_q0, pch_prob, pb, sc,
+                                         part_pt, cnt + nprob, it, max_inner, itol, cf, ext4,
+                                         nullptr);
     NB_CUDA(cudaGetLastError());
     NB_TRY(mark(mk ? mk + 2 : nullptr, s));
     return NB_OK;
   }
   int defect(double tol, int max_outer, cudaStream_t s, const cudaEvent_t *mk = nullptr) const {
+    if (paired()) {  // the x updates deferred by inner CGs that stopped mid-pair
+      k_bflush<<<npc, kThreads, 0, s>>>(e32, p32, pch_q0, pch_prob, sc);
+      NB_CUDA(cudaGetLastError());
+    }
     NB_TRY(launch_defect_ax(s));
     NB_TRY(mark(mk, s));
     k_bgs_res<<<ngc, kThreads, 0, s>>>(w, x, f, r, c, off, idx, gch_g0, gch_prob, pb, sc, part_gs,
@@ -882,7 +934,7 @@ struct Batch {
 
   int build_graph(double tol, int inner, int max_outer) {
     if (exec && tol == g_tol && inner == g_inner && max_outer == g_outer && itol == g_itol &&
-        wait_test_mode() == g_wtest && int(closed_c()) == g_cf)
+        wait_test_mode() == g_wtest && int(closed_c()) == g_cf && int(paired()) == g_pair)
       return NB_OK;
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -952,6 +1004,7 @@ struct Batch {
     g_itol = itol;
     g_wtest = wait_test_mode();
     g_cf = int(closed_c());
+    g_pair = int(paired());
     return NB_OK;
   }
 };
@@ -1091,6 +1144,8 @@ int batch_build(Batch *B, int nprob, const int *nx, const int *ny, const int *nz
   NB_TRY(dalloc(&B->r32, n));
   NB_TRY(dalloc(&B->e32, n));
   NB_TRY(dalloc(&B->p32, n));
+  NB_TRY(dalloc(&B->p32b, n));
+  NB_CUDA(cudaMemset(B->p32b, 0, n * sizeof(float)));
   NB_TRY(dalloc(&B->w32, n));
   NB_TRY(upload(&B->el_prob, el_prob));
   NB_TRY(upload(&B->off, off_all));

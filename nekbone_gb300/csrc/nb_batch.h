@@ -21,9 +21,12 @@ struct BatchScalars {
   double rtz1, rtz2, beta, pap, alpha, rtr;  // inner CG
   double rn0, rn;                            // |f|_C and current |r|_C (FP64)
   double irtr0;                              // the cycle's first inner r'Cr
+  double alpha_prev;                         // alpha of a deferred x update
   int active;                                // 1 while |r|/|f| > tol
   int outer, inner;                          // cycles and inner iterations
   int iactive;                               // 1 while the cycle's inner CG runs
+  int pend;                                  // the inner CG stopped with its
+                                             //   last x update deferred
 };
 
 // Per-problem index ranges into the concatenated batch arrays.
@@ -56,6 +59,9 @@ struct BaxArgs {
   T *w;
   const T *u;          // MODE 1: z
   T *p;                // MODE 1: search direction; MODE 2: x
+  const T *pold;       // MODE 1: the old direction, read from here (another
+                       //   buffer than p when the directions alternate; the
+                       //   launcher sets it to p when null)
   const T *g, *c, *D;
   const T *f;          // MODE 2
   T *r;                // MODE 2

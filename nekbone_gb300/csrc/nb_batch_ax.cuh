@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(LX * LX * EPB)
     if (act) {
       if (MODE == 1) {
         ureg[k] = a.u[id];
-        if (!a.first) pold[k] = a.p[id];
+        if (!a.first) pold[k] = a.pold[id];
       } else {
         ureg[k] = a.p[id];
         pold[k] = T(a.e[id]);
@@ -281,7 +281,7 @@ __global__ void __launch_bounds__(LX * LX)
     const size_t id = base + size_t(k) * L2 + t;
     if (MODE == 1) {
       ureg[k] = a.u[id];
-      pold[k] = a.first ? T(0) : a.p[id];
+      pold[k] = a.first ? T(0) : a.pold[id];
     } else {
       ureg[k] = a.p[id];
       pold[k] = T(a.e[id]);

@@ -143,29 +143,35 @@ def test_shapes_bit_identical(torch):
     b.close()
 
 
-@pytest.mark.parametrize("itol", [0.0, 1e-4])
-def test_closed_multiplicity_bit_identical(torch, itol):
-    """The inner CG with c formed in closed form (c verified at setup as
-    every problem's inverse multiplicity; the default) and with c read give
-    bit-identical solutions, per-problem results and cycle counts, with a
-    fixed inner count and with per-problem inner stops."""
+@pytest.mark.parametrize("itol,inner", [(0.0, 20), (1e-4, 30), (0.0, 7)])
+def test_inner_forms_bit_identical(torch, itol, inner):
+    """The inner CG's streamlined forms against the plain one: c formed in
+    closed form (verified at setup as every problem's inverse multiplicity)
+    or read, and the directions in two buffers with x updated once per pair
+    of iterations (problems that stop their inner CG on the first of a pair
+    get the deferred update before the defect; an odd inner count leaves the
+    last iteration unpaired) or one buffer.  Bit-identical solutions,
+    per-problem results and cycle counts."""
     import nekbone_gb300 as nb
     b = nb.Batch(BOXES)
     b.setup(23)
     b.set_inner_tol(itol)
     got = []
     try:
-        for closed in (True, False, True):
+        for closed, paired in ((True, True), (False, True), (True, False), (False, False),
+                               (True, True)):
             nb.set_mixed_closed_multiplicity(closed)
-            b.solve(1e-10, 20, 40)
+            nb.set_paired_update(paired)
+            b.solve(1e-10, inner, 40)
             nb.sync()
             x = _view(torch, b.arrays()[0], b.n).cpu().numpy().copy()
             got.append((x, [b.result(p) for p in range(b.nprob)], b.cycles()))
     finally:
         nb.set_mixed_closed_multiplicity(True)
-    for x, res, cyc in got[1:]:
-        assert np.array_equal(x, got[0][0])
-        assert res == got[0][1] and cyc == got[0][2]
+        nb.set_paired_update(True)
+    for k, (x, res, cyc) in enumerate(got[1:]):
+        assert np.array_equal(x, got[0][0]), k
+        assert res == got[0][1] and cyc == got[0][2], k
     b.close()
 
 
