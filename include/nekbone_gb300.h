@@ -183,14 +183,17 @@ void nb_set_shared_metric(int on);
  * products, update); 0 (default) the fused CUDA-core iteration.  The FP64
  * defect correction is the same either way, so both reach the tolerance. */
 void nb_set_mixed_tensor_cores(int on);
-/* CG (cg_, nb_cg: the fused FP64 iteration without preconditioner) and the
- * mixed solver's inner FP32 CG: 1 (default) keeps the search directions in
- * two buffers, odd and even iterations alternating, and updates x once per
- * two iterations (x += a_k p_k, then x += a_k+1 p_k+1, in one pass; the
- * last direction is copied to the caller's p); 0 one direction buffer and
- * an x update every iteration.  The same fused multiply-adds in the same
- * order either way (bitwise-equal results); the first form reads and
- * writes x half as often and takes n more values of device memory. */
+/* CG (cg_, nb_cg: the fused FP64 iteration without preconditioner), the
+ * mixed solver's inner FP32 CG and the batched solve's inner CG: 1
+ * (default) keeps the search directions in two buffers, odd and even
+ * iterations alternating, and updates x once per two iterations (x += a_k
+ * p_k, then x += a_k+1 p_k+1, in one pass; the last direction is copied to
+ * the caller's p; a batched problem whose inner CG stops mid-pair gets the
+ * deferred update before its defect); 0 one direction buffer and an x
+ * update every iteration.  The same fused multiply-adds in the same order
+ * either way (bitwise-equal results); the first form reads and writes x
+ * half as often and takes n more values of device memory.  A batch's
+ * graph is rebuilt when the switch changes. */
 void nb_set_paired_update(int on);
 /* Mixed solver and batched solve: 1 (default) checks whether the FP32 copy
  * of c is, bitwise at every point, a box mesh's inverse multiplicity (2^-m,

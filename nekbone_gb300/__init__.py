@@ -679,9 +679,10 @@ def set_mixed_tensor_cores(on: bool) -> None:
 
 
 def set_paired_update(on: bool) -> None:
-    """FP64 CG (fused, no preconditioner) and the mixed solver's inner FP32
-    CG: x updated once per two iterations from two direction buffers (True,
-    default) or every iteration (False); bitwise the same iterates."""
+    """FP64 CG (fused, no preconditioner), the mixed solver's inner FP32 CG
+    and the batched solve's inner CG: x updated once per two iterations from
+    two direction buffers (True, default) or every iteration (False);
+    bitwise the same iterates."""
     lib.nb_set_paired_update(1 if on else 0)
 
 
