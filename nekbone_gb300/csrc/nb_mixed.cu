@@ -209,10 +209,12 @@ void set_shared_metric(bool on) { g_shared_metric = on; }
 // split operands, FP32 accumulation) instead of the fused CUDA-core pass
 bool g_mixed_tc = false;
 // x updated once per two iterations from two direction buffers (the FP64
-// CG's and the inner CG's p_alt; bitwise the same iterates)
+// CG, the mixed solver's inner CG and the batched solve's inner CG;
+// bitwise the same iterates)
 bool g_paired_update = true;
-// the inner CG forms c in closed form where c verifies as a box mesh's
-// inverse multiplicity (c_closed_form; the same values)
+// the inner CGs (this solver's and the batched solve's) form c in closed
+// form where c verifies as a box mesh's inverse multiplicity (the same
+// values)
 bool g_mixed_closed_c = true;
 
 // flag: one device int of scratch
