@@ -796,11 +796,17 @@ int time_cg_kernels_t(Operator &op, CgWork &wk, T *x, const T *f, const T *g,
   const int iters = PAIRED ? 2 * reps : reps;
   T *p_alt = nullptr;
   unsigned char *cface = nullptr;
-  if (PAIRED) NB_CUDA(cudaMalloc(&p_alt, op.n * sizeof(T)));
-  if (F32 && g_mixed_closed_c) NB_CUDA(cudaMalloc(&cface, size_t(op.nelt) + 16));
-  std::unique_ptr<T, int (*)(T *)> p_alt_owner(p_alt, [](T *q) { return int(cudaFree(q)); });
+  std::unique_ptr<T, int (*)(T *)> p_alt_owner(nullptr, [](T *q) { return int(cudaFree(q)); });
   std::unique_ptr<unsigned char, int (*)(unsigned char *)> cface_owner(
-      cface, [](unsigned char *q) { return int(cudaFree(q)); });
+      nullptr, [](unsigned char *q) { return int(cudaFree(q)); });
+  if (PAIRED) {
+    NB_CUDA(cudaMalloc(&p_alt, op.n * sizeof(T)));
+    p_alt_owner.reset(p_alt);
+  }
+  if (F32 && g_mixed_closed_c) {
+    NB_CUDA(cudaMalloc(&cface, size_t(op.nelt) + 16));
+    cface_owner.reset(cface);
+  }
   struct FaceReset {
     CgWork &wk;
     ~FaceReset() { wk.c32_face = nullptr; }
