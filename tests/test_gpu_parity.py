@@ -459,6 +459,38 @@ def test_cg_paired_update_bitwise(nb, niter, order):
     assert np.array_equal(outs[True][1], outs[False][1])
 
 
+def test_kernel_timing_entry_points(nb):
+    """nb_time_cg_kernels and nb_time_cg_kernels_f32 run the solvers' forms
+    (paired x update on and off; FP32 with c formed in closed form) and
+    report a positive time for each of the iteration's three kernels."""
+    torch = pytest.importorskip("torch")
+    m = nb.DeviceMesh(4, 4, 4, 8, mask_mode=1)
+    dev = torch.device("cuda")
+    n = m.n
+    g = torch.empty(6 * n, dtype=torch.float64, device=dev)
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    f = torch.empty(n, dtype=torch.float64, device=dev)
+    m.setup_g(g.data_ptr())
+    m.set_multiplicity(c.data_ptr())
+    m.rhs_uniform(f.data_ptr(), c.data_ptr(), 3)
+    g32, c32, f32 = g.float(), c.float(), f.float()
+    try:
+        for paired in (True, False):
+            nb.set_paired_update(paired)
+            v = [torch.zeros(n, dtype=torch.float64, device=dev) for _ in range(4)]
+            ms = m.time_cg_kernels(v[0].data_ptr(), f.data_ptr(), g.data_ptr(), c.data_ptr(),
+                                   v[1].data_ptr(), v[2].data_ptr(), v[3].data_ptr(), reps=2)
+            v32 = [torch.zeros(n, dtype=torch.float32, device=dev) for _ in range(4)]
+            ms32 = m.time_cg_kernels_f32(v32[0].data_ptr(), f32.data_ptr(), g32.data_ptr(),
+                                         c32.data_ptr(), v32[1].data_ptr(), v32[2].data_ptr(),
+                                         v32[3].data_ptr(), reps=2)
+            assert len(ms) == 3 and all(t > 0 for t in ms), (paired, ms)
+            assert len(ms32) == 3 and all(t > 0 for t in ms32), (paired, ms32)
+            assert torch.isfinite(v[0]).all() and torch.isfinite(v32[0]).all()
+    finally:
+        nb.set_paired_update(True)
+
+
 def test_mixed_closed_multiplicity_rejects_other_c(nb):
     """A c that is not the box's inverse multiplicity (one point changed)
     fails the closed-form check, and the inner CG reads it: the solve
